@@ -1,0 +1,400 @@
+"""Benchmark: eSRRF input Mpx*frames/s on one GB300 (and N independent replicas).
+
+Workload (default): the large single eSRRF -- 500 frames x 512 x 512 float32
+(seeded blinking emitters, 400 emitters), magnification 5, radius 1.5,
+sensitivity 2, VAR and TAC2 correlations, 100 frames per timepoint,
+macro-pixel correction; output 2 x 5 x 2560 x 2560 float32.
+
+* ``value``: device-resident throughput (input already in HBM): one step = the
+  full reconstruction of the stack (fused frame-loop kernel + temporal
+  finalisation + macro-pixel correction), CUDA events on the launching stream.
+* ``e2e``: the same reconstruction through the public API ``nanopyx_gb300.eSRRF``
+  with NumPy host buffers in and out (H2D + D2H inside the timed region).
+* ``roofline``: the fused kernel's algorithmic FP32 FLOP/s over the measured
+  FP32 FMA peak of this GPU (the path is FP32-compute bound; no tensor cores).
+* ``cpu_baseline``: the reference's own compiled CPU path (``oracle/_ref``) on a
+  bounded sample of the same workload, all host threads.
+
+``--impl reference`` times the reference CPU path alone (rank 0 only).
+Inputs (524 MB) are larger than L2 (129 MB), so no L2 flush is needed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+CFG = dict(T=500, H=512, W=512, emitters=400, m=5, radius=1.5, sensitivity=2.0,
+           correlations=("VAR", "TAC2"), fpt=100, mpc=True, seed=1)
+METRIC = "eSRRF input Mpx*frames/s"
+REF_SAMPLE_FRAMES = 4
+
+
+def _workload_name():
+    return (f"large single eSRRF {CFG['T']}x{CFG['H']}x{CFG['W']} m={CFG['m']} R={CFG['radius']} "
+            f"s={CFG['sensitivity']:g} VAR+TAC2 fpt={CFG['fpt']} MPC")
+
+
+def _mpx_frames(T, H, W):
+    return T * H * W / 1e6
+
+
+def make_stack():
+    from nanopyx_gb300.synthetic import blinking_stack
+
+    return blinking_stack(CFG["T"], CFG["H"], CFG["W"], CFG["emitters"], seed=CFG["seed"])
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
+        except Exception:
+            return None
+        rows = [r for r in rows if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        busy = [s for s in sm if s > 0.5 * mx] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic work of the fused kernel
+# ---------------------------------------------------------------------------
+def samples_per_output(m, radius):
+    """Mean number of in-radius RGC samples per output pixel, S(m, R)."""
+    import ctypes
+
+    from nanopyx_gb300 import _native
+
+    L = _native.lib()
+    cap = m * m * 64 * 64
+    buf = np.zeros(cap, dtype=np.float32)
+    J = L.nx_esrrf_weight_table(m, float(radius), buf.ctypes.data_as(ctypes.c_void_p), cap)
+    W2 = 2 * J + 1
+    w = buf[: m * m * W2 * W2]
+    return float((w > 0).sum()) / (m * m)
+
+
+def fused_flops(T, H, W, m, radius):
+    """FLOP = sum_frames [H W m^2 (10 S(m,R) + 20) + 60 H W]."""
+    S = samples_per_output(m, radius)
+    return T * (H * W * m * m * (10.0 * S + 20.0) + 60.0 * H * W), S
+
+
+def measure_fp32_peak(device):
+    import torch
+
+    from nanopyx_gb300 import _native
+
+    L = _native.lib()
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks = sms * 8
+    iters = 4096
+    sink = torch.empty(blocks * 256, dtype=torch.float32, device=device)
+    s = torch.cuda.current_stream(device)
+    for _ in range(2):
+        _native.check(L.nx_probe_ffma(sink.data_ptr(), blocks, iters, s.cuda_stream))
+    torch.cuda.synchronize(device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record(s)
+        _native.check(L.nx_probe_ffma(sink.data_ptr(), blocks, iters, s.cuda_stream))
+        e1.record(s)
+        torch.cuda.synchronize(device)
+        flops = blocks * 256 * iters * 16 * 8 * 2.0
+        best = max(best, flops / (e0.elapsed_time(e1) * 1e-3))
+    return best / 1e12
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's compiled path on a bounded sample
+# ---------------------------------------------------------------------------
+def reference_step(R, sample):
+    """eSRRF_ST + VAR + TAC2 + macro-pixel correction on one sample block."""
+    st = R["eSRRF_ST"](verbose=False).run(sample, magnification=CFG["m"], radius=CFG["radius"],
+                                          sensitivity=CFG["sensitivity"], run_type="Threaded")
+    outs = []
+    for corr in CFG["correlations"]:
+        tc = R["calculate_eSRRF_temporal_correlations"](st, corr)
+        outs.append(R["macro_pixel_corrector"](np.expand_dims(np.asarray(tc), 0),
+                                               magnification=CFG["m"]))
+    return outs
+
+
+def cpu_reference_available():
+    try:
+        from oracle import ref_build
+
+        if not ref_build.available():
+            ref_build.build()
+        return ref_build.available()
+    except Exception:
+        return False
+
+
+def time_cpu_baseline(stack, frames=REF_SAMPLE_FRAMES):
+    """Returns the cpu_baseline dict (reference if buildable here, else the FP64 port)."""
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    sample = np.ascontiguousarray(stack[:frames])
+    if cpu_reference_available():
+        from oracle import ref_build
+
+        R = ref_build.load()
+        reference_step(R, sample[:1])  # warm-up (thread pool, pages)
+        t0 = time.perf_counter()
+        reference_step(R, sample)
+        dt = time.perf_counter() - t0
+        kind = "reference"
+        desc = (f"{frames} frames of the {CFG['H']}x{CFG['W']} stack as one timepoint: "
+                f"compiled reference eSRRF_ST(Threaded) + VAR + TAC2 + macro_pixel_corrector")
+    else:
+        from oracle import esrrf_np
+
+        frames = 1
+        cores = 1
+        t0 = time.perf_counter()
+        esrrf_np.esrrf_st(sample[:1], CFG["m"], CFG["radius"], CFG["sensitivity"])
+        dt = time.perf_counter() - t0
+        kind = "port"
+        desc = "1 frame of the stack through the FP64 NumPy oracle (reference not buildable)"
+    return {"value": _mpx_frames(frames, CFG["H"], CFG["W"]) / dt, "unit": "Mpx*frames/s",
+            "cores": int(os.environ.get("OMP_NUM_THREADS", cores)) if kind == "reference" else 1,
+            "kind": kind, "sample": desc, "seconds": dt}
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(cores)
+    from nanopyx_gb300.synthetic import blinking_stack
+
+    frames = REF_SAMPLE_FRAMES
+    stack = blinking_stack(frames, CFG["H"], CFG["W"], CFG["emitters"], seed=CFG["seed"])
+    line = {"impl": "reference", "metric": METRIC, "unit": "Mpx*frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": _workload_name(), "parallelism": "cpu"}}
+    if not cpu_reference_available():
+        from oracle import esrrf_np
+
+        kind, cores_used = "port", 1
+        fn = lambda: esrrf_np.esrrf_st(stack[:1], CFG["m"], CFG["radius"], CFG["sensitivity"])  # noqa: E731
+        frames = 1
+        sample = "1 frame per step through the FP64 NumPy oracle (reference not buildable here)"
+    else:
+        from oracle import ref_build
+
+        R = ref_build.load()
+        kind, cores_used = "reference", cores
+        fn = lambda: reference_step(R, stack)  # noqa: E731
+        sample = (f"{frames} frames of the {CFG['H']}x{CFG['W']} stack per step as one timepoint: "
+                  "eSRRF_ST(Threaded) + VAR + TAC2 + macro_pixel_corrector")
+    for _ in range(args.warmup):
+        fn()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        fn()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = _mpx_frames(frames, CFG["H"], CFG["W"]) / (ms / 1e3)
+    line.update({"value": value, "ms_per_step": ms,
+                 "cpu_baseline": {"value": value, "unit": "Mpx*frames/s", "cores": cores_used,
+                                  "kind": kind, "sample": sample},
+                 "e2e": {"value": value, "unit": "Mpx*frames/s", "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": 0}})
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu_arm(args):
+    import torch
+
+    import nanopyx_gb300 as nx
+    from nanopyx_gb300 import _device, _native
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    stack_np = make_stack()
+    T, H, W = stack_np.shape
+    m, R, s = CFG["m"], CFG["radius"], CFG["sensitivity"]
+    fpt = CFG["fpt"]
+    L = _native.lib()
+    stream = torch.cuda.current_stream(dev)
+    x = torch.from_numpy(stack_np).to(dev)
+    plan = _device.get_plan(H, W, m, R, s, True)
+    mask = _native.NX_CORR_VAR | _native.NX_CORR_TAC2
+    ws = _device.workspace(L.nx_esrrf_workspace_bytes(plan.handle, T, fpt, mask), dev)
+    n_tp = (T + fpt - 1) // fpt
+    out = torch.empty((2, n_tp, H * m, W * m), dtype=torch.float32, device=dev)
+
+    def step(ev0=None, ev1=None):
+        if ev0 is not None:
+            ev0.record(stream)
+        _native.check(L.nx_esrrf_run_stage1(plan.handle, x.data_ptr(), T, fpt, mask,
+                                            ws.data_ptr(), ws.numel(), stream.cuda_stream))
+        if ev1 is not None:
+            ev1.record(stream)
+        _native.check(L.nx_esrrf_run_stage2(plan.handle, T, fpt, mask, 1, out.data_ptr(),
+                                            ws.data_ptr(), ws.numel(), stream.cuda_stream))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    _native.check(L.nx_workspace_status(ws.data_ptr(), stream.cuda_stream), "warm-up")
+
+    k_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in range(args.steps)]
+    t_start, t_stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        t_start.record(stream)
+        for i in range(args.steps):
+            step(*k_ev[i])
+        t_stop.record(stream)
+        torch.cuda.synchronize(dev)
+    if dist is not None:
+        dist.barrier()
+    _native.check(L.nx_workspace_status(ws.data_ptr(), stream.cuda_stream), "timed steps")
+    total_ms = t_start.elapsed_time(t_stop)
+    kern_ms = sum(a.elapsed_time(b) for a, b in k_ev) / args.steps
+    if dist is not None:
+        tt = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / args.steps
+    mpxf = _mpx_frames(T, H, W)
+    value = world * mpxf / (ms_per_step / 1e3)
+
+    # kernel roofline (FP32 FMA bound)
+    flops, S = fused_flops(T, H, W, m, R)
+    achieved = flops / (kern_ms * 1e-3) / 1e12
+    peak = measure_fp32_peak(dev)
+    clocks = clk.summary()
+
+    # end to end through the public API with host buffers
+    e2e_times = []
+    for i in range(max(1, min(args.steps, 3)) + 1):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res = nx.eSRRF(stack_np, magnification=m, radius=R, sensitivity=s,
+                       frames_per_timepoint=fpt, temporal_correlation=CFG["correlations"])
+        t1 = time.perf_counter()
+        if i > 0:
+            e2e_times.append(t1 - t0)
+    e2e_s = statistics.median(e2e_times)
+    out_bytes = sum(r.nbytes for r in res)
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpx*frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded blinking emitters)",
+        "config": {"workload": _workload_name(), "T": T, "H": H, "W": W, "magnification": m,
+                   "radius": R, "sensitivity": s, "correlations": list(CFG["correlations"]),
+                   "frames_per_timepoint": fpt, "macro_pixel_correction": True,
+                   "parallelism": f"replicas{world}" if world > 1 else "single GPU",
+                   "l2": "input 524 MB > 129 MB L2; no flush"},
+        "e2e": {"value": mpxf / e2e_s, "unit": "Mpx*frames/s", "seconds": e2e_s,
+                "h2d_bytes_per_step": int(stack_np.nbytes), "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": args.steps * (1 + n_tp + 2),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "esrrf_fused_kernel<5,3,2,FULL>", "kernel_ms": kern_ms,
+                     "flops_per_launch": flops, "samples_per_output": S,
+                     "peak_source": "measured FFMA-loop throughput on this GPU (no FP32 figure "
+                                    "in MEASURED_PEAKS.json)"},
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = time_cpu_baseline(stack_np)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

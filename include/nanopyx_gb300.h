@@ -1,0 +1,174 @@
+/*
+ * nanopyx_gb300.h -- C ABI of the GB300 (sm_103a) eSRRF / SRRF engine.
+ *
+ * Plain pointers and sizes only: every `d_*` argument is a CUDA device
+ * pointer, every `stream` argument is a cudaStream_t passed as void* (NULL =
+ * the legacy default stream), every function returns an int status (NX_OK or
+ * a negative NX_ERR_* code; nx_last_error() gives the message of the last
+ * failure on the calling thread).  All compute calls are asynchronous on
+ * `stream`; arrays are float32, C-contiguous, frames outermost.
+ *
+ * Each entry point names the reference routine it replaces (paths inside the
+ * NanoPyx project).  The Python package nanopyx_gb300 binds these through
+ * ctypes and re-exposes the reference's Liquid-Engine call surface on top.
+ */
+#ifndef NANOPYX_GB300_H
+#define NANOPYX_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NX_ABI_VERSION 1
+
+/* status codes */
+#define NX_OK 0
+#define NX_ERR_INVALID_ARG (-1)     /* bad shape / parameter (reference: ValueError) */
+#define NX_ERR_UNSUPPORTED (-2)     /* valid request this build does not implement */
+#define NX_ERR_OUT_OF_MEMORY (-3)   /* device allocation failed (reference: cl.MemoryError retry) */
+#define NX_ERR_CUDA (-4)            /* CUDA runtime error */
+#define NX_ERR_DEVICE_TIMEOUT (-5)  /* a bounded device wait ran out (kernel returned early) */
+#define NX_ERR_WORKSPACE (-6)       /* workspace missing or too small */
+
+/* temporal correlations (bit mask; outputs are written in this order) */
+#define NX_CORR_AVG 1
+#define NX_CORR_VAR 2
+#define NX_CORR_TAC2 4
+
+typedef struct nx_esrrf_plan nx_esrrf_plan;
+
+int nx_abi_version(void);
+const char* nx_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * eSRRF plan: per-(H, W, magnification, radius, sensitivity, weighting)
+ * constants (FP64-derived phase tables of the RGC distance weights, the
+ * clamped-edge Catmull-Rom taps) uploaded once to the device.
+ * Replaces the per-call parameter set-up of
+ *   src/nanopyx/core/transform/_le_radial_gradient_convergence.pyx:85-104
+ * ------------------------------------------------------------------------ */
+int nx_esrrf_plan_create(nx_esrrf_plan** plan, int H, int W, int magnification, float radius,
+                         float sensitivity, int do_intensity_weighting);
+int nx_esrrf_plan_destroy(nx_esrrf_plan* plan);
+
+/* Host-only (no device call): the RGC distance-weight phase table a plan
+ * uploads, w[py][px][j][i] for output sub-pixel phase (py, px) and half-grid
+ * window offset (j, i) in [-J, J]; returns J (or a negative status).  Writes
+ * nothing if `cap` (floats) is smaller than magnification^2 (2J+1)^2.
+ *   src/include/_c_sr_radial_gradient_convergence.c:4-6,27-64                */
+int nx_esrrf_weight_table(int magnification, float radius, float* h_out, size_t cap);
+
+/* Per-frame RGC stack (T, H*m, W*m): the output of eSRRF_ST.run
+ *   src/nanopyx/core/transform/_le_esrrf.pyx:30-33,172-196                 */
+size_t nx_esrrf_st_workspace_bytes(const nx_esrrf_plan* plan, int T);
+int nx_esrrf_st(const nx_esrrf_plan* plan, const float* d_in, int T, float* d_out, void* d_ws,
+                size_t ws_bytes, void* stream);
+
+/* Full eSRRF(): per timepoint block of `frames_per_timepoint` frames (0 = all),
+ * the temporal correlations in `corr_mask` and, if `macro_pixel_correction`,
+ * the macro-pixel correction.  d_out is (n_corr, n_timepoints, H*m, W*m).
+ *   src/nanopyx/methods/esrrf/eSRRF_workflow.py:58-121
+ *   src/nanopyx/core/transform/sr_temporal_correlations.py:46-75,205-221
+ *   src/nanopyx/core/transform/mpcorrector.pyx:7-73                          */
+size_t nx_esrrf_workspace_bytes(const nx_esrrf_plan* plan, int T, int frames_per_timepoint,
+                                int corr_mask);
+int nx_esrrf_run(const nx_esrrf_plan* plan, const float* d_in, int T, int frames_per_timepoint,
+                 int corr_mask, int macro_pixel_correction, float* d_out, void* d_ws,
+                 size_t ws_bytes, void* stream);
+
+/* The two stages of nx_esrrf_run, for callers that time or overlap them:
+ * stage 1 runs the fused frame-loop kernel (per-timepoint temporal sums into
+ * the workspace), stage 2 turns them into the correlations (+ macro-pixel
+ * correction).  Same workspace, same arguments.                              */
+int nx_esrrf_run_stage1(const nx_esrrf_plan* plan, const float* d_in, int T,
+                        int frames_per_timepoint, int corr_mask, void* d_ws, size_t ws_bytes,
+                        void* stream);
+int nx_esrrf_run_stage2(const nx_esrrf_plan* plan, int T, int frames_per_timepoint,
+                        int corr_mask, int macro_pixel_correction, float* d_out, void* d_ws,
+                        size_t ws_bytes, void* stream);
+
+/* Throughput probe (not a reference routine): `blocks` CTAs of 256 threads
+ * each run `iters` iterations of 8 independent FP32 FMA chains; returns via
+ * d_sink (blocks*256 floats) so nothing is optimised away.  Used to measure
+ * the FP32 FMA peak the RGC kernel is compared against.                       */
+int nx_probe_ffma(float* d_sink, int blocks, int iters, void* stream);
+
+/* Streaming accumulation for served requests: frame blocks of one
+ * reconstruction are pushed as they arrive; the device-resident accumulator
+ * (nx_esrrf_accum_bytes) holds the per-pixel temporal state between pushes.
+ * Finalize writes (n_corr, H*m, W*m).  Same arithmetic as nx_esrrf_run with
+ * one timepoint.  (No single reference counterpart: the reference keeps the
+ * whole per-frame stack in host RAM, eSRRF_workflow.py:76-112.)              */
+size_t nx_esrrf_accum_bytes(const nx_esrrf_plan* plan);
+size_t nx_esrrf_push_workspace_bytes(const nx_esrrf_plan* plan, int T_block);
+int nx_esrrf_accum_push(const nx_esrrf_plan* plan, const float* d_block, int T_block,
+                        int frames_before, void* d_accum, void* d_ws, size_t ws_bytes,
+                        void* stream);
+int nx_esrrf_accum_finalize(const nx_esrrf_plan* plan, const void* d_accum, int total_frames,
+                            int corr_mask, int macro_pixel_correction, float* d_out, void* d_ws,
+                            size_t ws_bytes, void* stream);
+
+/* Device status word check (synchronises `stream`): returns NX_OK or
+ * NX_ERR_DEVICE_TIMEOUT if a kernel of a previous call on this workspace
+ * recorded a bounded-wait timeout.                                          */
+int nx_workspace_status(const void* d_ws, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Standalone Liquid-Engine ops of the path
+ * ------------------------------------------------------------------------ */
+
+/* Catmull-Rom ShiftAndMagnify; per-frame shifts (length T, device arrays).
+ *   src/nanopyx/core/transform/_le_interpolation_catmull_rom.pyx:17,143-160
+ *   src/include/_c_interpolation_catmull_rom.c:6-52
+ * d_out is (T, (int)(H*mag_row), (int)(W*mag_col)).                        */
+int nx_cr_shift_magnify(const float* d_in, int T, int H, int W, const float* d_shift_row,
+                        const float* d_shift_col, float mag_row, float mag_col, float* d_out,
+                        void* stream);
+
+/* Roberts-Cross gradients (gradient_col, gradient_row), each (T, H, W).
+ *   src/nanopyx/core/transform/_le_roberts_cross_gradients.pyx:67-83
+ *   src/include/_c_gradients.c:53-73                                        */
+int nx_roberts_cross(const float* d_in, int T, int H, int W, float* d_gc, float* d_gr,
+                     void* stream);
+
+/* Radial Gradient Convergence on given 2m-magnified gradients
+ * (T, 2*rowsM, 2*colsM) and m-magnified image (T, rowsM, colsM).
+ *   src/nanopyx/core/transform/_le_radial_gradient_convergence.pyx:28,79-115
+ *   src/include/_c_sr_radial_gradient_convergence.c:4-90                    */
+int nx_rgc(const float* d_gc_interp, const float* d_gr_interp, const float* d_img_interp, int T,
+           int rowsM, int colsM, int magnification, float radius, float sensitivity,
+           int do_intensity_weighting, int pad_edges, float* d_out, void* stream);
+
+/* SRRF radiality: d_img (T, h, w), d_img_interp (T, h*m, w*m) -> (T, h*m, w*m).
+ *   src/nanopyx/core/transform/_le_radiality.pyx:86-125
+ *   src/include/_c_sr_radiality.c:6-51, src/include/_c_gradients.c:3-25     */
+size_t nx_radiality_workspace_bytes(int T, int h, int w);
+int nx_radiality(const float* d_img, const float* d_img_interp, int T, int h, int w,
+                 int magnification, float ring_radius, int border, int positivity_constraint,
+                 int do_intensity_weighting, float* d_out, void* d_ws, size_t ws_bytes,
+                 void* stream);
+
+/* eSRRF temporal correlation of a stack (T, n_pixels) -> (n_pixels).
+ *   src/nanopyx/core/transform/sr_temporal_correlations.py:46-75,205-221    */
+int nx_temporal_correlation(const float* d_stack, int T, long long n_pixels, int correlation,
+                            float* d_out, void* stream);
+
+/* SRRF temporal correlation orders 0 (max), 1 (mean), -1 (pairwise product
+ * sum), 2/3/4 (ACRF, without lag-time integration).
+ *   src/nanopyx/core/transform/sr_temporal_correlations.py:4-43,78-202      */
+int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n_pixels, int order,
+                                 float* d_out, void* stream);
+
+/* Macro-pixel correction in place on (S, rowsM, colsM).
+ *   src/nanopyx/core/transform/mpcorrector.pyx:7-73                         */
+size_t nx_macro_pixel_workspace_bytes(int S, int magnification);
+int nx_macro_pixel_correct(float* d_img, int S, int rowsM, int colsM, int magnification,
+                           void* d_ws, size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NANOPYX_GB300_H */

@@ -1,0 +1,757 @@
+// C-ABI of the eSRRF / SRRF engine: plans, workspace sizing, dispatch.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+#include "nanopyx_gb300.h"
+
+namespace nx {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int cuda_status(cudaError_t e, const char* what) {
+  set_error("%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? NX_ERR_OUT_OF_MEMORY : NX_ERR_CUDA;
+}
+
+static int invalid(const char* msg) {
+  set_error("%s", msg);
+  return NX_ERR_INVALID_ARG;
+}
+
+// ---------------------------------------------------------------------------
+// fused-kernel registry
+// ---------------------------------------------------------------------------
+const FusedEntry* fused_entry(int M, int J) {
+  switch (M) {
+    case 1: return fused_entry_m1(J);
+    case 2: return fused_entry_m2(J);
+    case 3: return fused_entry_m3(J);
+    case 4: return fused_entry_m4(J);
+    case 5: return fused_entry_m5(J);
+    case 6: return fused_entry_m6(J);
+    case 8: return fused_entry_m8(J);
+    default: return nullptr;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// TMA descriptor encoding through the driver entry point (no libcuda link)
+// ---------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// 3-D (W, H, T) float32 map with a (BW, BH, 1) box, zero fill out of bounds.
+static bool make_frame_tmap(CUtensorMap* map, const float* base, int T, int H, int W, int BW,
+                            int BH) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
+  if (((size_t)W * 4) % 16 != 0) return false;
+  if (BW > 256 || BH > 256 || (BW * 4) % 16 != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)T};
+  const cuuint64_t strides[2] = {(cuuint64_t)W * 4, (cuuint64_t)W * H * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)BW, (cuuint32_t)BH, 1u};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+static int g_force_no_tma = -1;
+static bool tma_disabled() {
+  if (g_force_no_tma < 0) {
+    const char* e = getenv("NANOPYX_GB300_NO_TMA");
+    g_force_no_tma = (e && *e && *e != '0') ? 1 : 0;
+  }
+  return g_force_no_tma == 1;
+}
+
+static int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 148;
+  return sms > 0 ? sms : 148;
+}
+
+}  // namespace nx
+
+// ---------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------
+struct nx_esrrf_plan {
+  int H, W, M;
+  float radius, sensitivity;
+  int iw;
+  int rowsM, colsM;
+  int JW;           // half-width of the (symmetric) window used by the fused kernel
+  nx::RgcScalars sc;
+  const nx::FusedEntry* fused;
+  int cy_base, cx_base;
+  float cy[4], cx[4];
+  int device;
+  float* d_tbl;     // device: [tbl | inv_wsum | wfull]
+  size_t n_tbl, n_inv, n_wfull;
+};
+
+namespace nx {
+
+// Catmull-Rom taps (double, as _c_cubic) of the 2m-grid index 2*m*n-1 along an
+// axis of n input pixels: the position the reference RGC clamps to.
+static void clamp_taps(int n, int M, int* base, float w[4]) {
+  const float mag = (float)(2 * M);
+  const float r = (float)(2 * M * n - 1) / mag;  // float division, as ShiftAndMagnify
+  const int r_int = (int)std::floor((float)((double)r - 0.5));
+  *base = r_int - 1;
+  for (int t = 0; t < 4; ++t) {
+    const int nb = r_int - 1 + t;
+    double v = std::fabs((double)r - ((double)nb + 0.5));
+    double z = 0.0;
+    if (v < 1) z = v * v * (v * (-0.5 + 2) + (0.5 - 3)) + 1;
+    else if (v < 2) z = -0.5 * v * v * v + 5 * 0.5 * v * v - 8 * 0.5 * v + 4 * 0.5;
+    w[t] = (nb >= 0 && nb < n) ? (float)z : 0.f;
+  }
+}
+
+// Phase tables of the RGC sample weights (FP64, rounded once to float).
+//   per output sub-pixel phase (py, px) and window offset (j, i):
+//   dx, dy: offset of the half-grid sample from the output centre,
+//   d = |(dx, dy)|, w = (d exp(-d^2 / tSS))^4 if 0 < d <= tSO, else 0,
+//   a = dx * w / d, b = dy * w / d.
+static void build_tables(nx_esrrf_plan* p, std::vector<float>& tbl, std::vector<float>& inv,
+                         std::vector<float>& wfull) {
+  const int M = p->M;
+  const int JW = p->JW;
+  const int W2 = 2 * JW + 1;
+  const int NS = M * W2;
+  const int NS4 = (NS + 3) / 4;
+  tbl.assign((size_t)M * W2 * 3 * NS4 * 4, 0.f);
+  inv.assign((size_t)M * M, 0.f);
+  wfull.assign((size_t)M * M * W2 * W2, 0.f);
+  const double tSS = p->sc.tSS, tSO = p->sc.tSO;
+  std::vector<double> wsum((size_t)M * M, 0.0);
+  for (int py = 0; py < M; ++py) {
+    const int cpy = (2 * py + 1) / M;
+    for (int jj = 0; jj < W2; ++jj) {
+      const int j = jj - JW;
+      const double dy = (cpy + j) / 2.0 - (py + 0.5) / M;
+      float* blk = tbl.data() + (size_t)(py * W2 + jj) * 3 * NS4 * 4;
+      for (int px = 0; px < M; ++px) {
+        const int cpx = (2 * px + 1) / M;
+        for (int ii = 0; ii < W2; ++ii) {
+          const int i = ii - JW;
+          const double dx = (cpx + i) / 2.0 - (px + 0.5) / M;
+          const float d = (float)std::sqrt(dx * dx + dy * dy);
+          const bool in_win = j >= p->sc.start && j < p->sc.end && i >= p->sc.start &&
+                              i < p->sc.end;
+          float w = 0.f, a = 0.f, b = 0.f;
+          if (in_win && d != 0.f && d <= p->sc.tSO) {
+            const double dd = d;
+            const double e = dd * std::exp(-(dd * dd) / tSS);
+            w = (float)(e * e * e * e);
+            const double wd = (double)w / dd;
+            a = (float)(dx * wd);
+            b = (float)(dy * wd);
+          }
+          (void)tSO;
+          const int sidx = px * W2 + ii;
+          blk[0 * NS4 * 4 + sidx] = a;
+          blk[1 * NS4 * 4 + sidx] = b;
+          blk[2 * NS4 * 4 + sidx] = w;
+          wfull[((size_t)(py * M + px) * W2 + jj) * W2 + ii] = w;
+          wsum[py * M + px] += (double)w;
+        }
+      }
+    }
+  }
+  for (int k = 0; k < M * M; ++k) inv[k] = wsum[k] > 0 ? (float)(1.0 / (double)(float)wsum[k]) : 0.f;
+}
+
+static int check_plan(const nx_esrrf_plan* p) {
+  if (!p) return invalid("plan is NULL");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != p->device) {
+    set_error("plan was created on device %d but device %d is current", p->device, dev);
+    return NX_ERR_INVALID_ARG;
+  }
+  return NX_OK;
+}
+
+// chunking of each timepoint's frames across CTAs (deterministic in its inputs)
+static int plan_chunks(const nx_esrrf_plan* p, int T, int fpt, int n_tp) {
+  if (!p->fused) return 1;
+  const int TY = p->fused->geo.TY;
+  const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + TY - 1) / TY);
+  const int min_nf = std::min(fpt, T - (n_tp - 1) * fpt);
+  const long long target = 3LL * device_sms();
+  long long c = (target + tiles * n_tp - 1) / (tiles * n_tp);
+  c = std::min<long long>(c, std::max(1, min_nf / 4));
+  c = std::max<long long>(1, std::min<long long>(c, min_nf));
+  return (int)c;
+}
+
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+static const size_t kStatusBytes = 256;
+
+static int corr_count(int mask) {
+  return ((mask & NX_CORR_AVG) ? 1 : 0) + ((mask & NX_CORR_VAR) ? 1 : 0) +
+         ((mask & NX_CORR_TAC2) ? 1 : 0);
+}
+
+static int fields_for(int corr_mask) {
+  return (corr_mask & (NX_CORR_VAR | NX_CORR_TAC2)) ? 5 : 2;
+}
+
+static void fill_params(const nx_esrrf_plan* p, FusedParams& fp, const float* in, int T, int fpt,
+                        int n_tp, int chunks, float* out, unsigned* status) {
+  memset(&fp, 0, sizeof(fp));
+  fp.in = in;
+  fp.T = T;
+  fp.H = p->H;
+  fp.W = p->W;
+  fp.rowsM = p->rowsM;
+  fp.colsM = p->colsM;
+  fp.tiles_x = (p->W + 31) / 32;
+  fp.fpt = fpt;
+  fp.n_tp = n_tp;
+  fp.chunks = chunks;
+  fp.margin = p->sc.margin;
+  fp.iw = p->iw;
+  fp.sens_mode = p->sc.sens_mode;
+  fp.sens_int = p->sc.sens_int;
+  fp.sens = p->sc.sens;
+  fp.cy_base = p->cy_base;
+  fp.cx_base = p->cx_base;
+  for (int t = 0; t < 4; ++t) {
+    fp.cy[t] = p->cy[t];
+    fp.cx[t] = p->cx[t];
+  }
+  fp.tbl = p->d_tbl;
+  fp.inv_wsum = p->d_tbl + p->n_tbl;
+  fp.wfull = p->d_tbl + p->n_tbl + p->n_inv;
+  fp.out = out;
+  fp.status = status;
+}
+
+static int launch_fused_mode(const nx_esrrf_plan* p, int mode, const float* d_in, int T, int fpt,
+                             int n_tp, int chunks, float* out, unsigned* status,
+                             cudaStream_t s) {
+  FusedParams fp;
+  fill_params(p, fp, d_in, T, fpt, n_tp, chunks, out, status);
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  fp.use_tma = 0;
+  if (!tma_disabled() && make_frame_tmap(&tmap, d_in, T, p->H, p->W, p->fused->geo.BW,
+                                         p->fused->geo.BH))
+    fp.use_tma = 1;
+  cudaError_t e = p->fused->launch[mode](fp, tmap, s);
+  if (e != cudaSuccess) return cuda_status(e, "fused eSRRF launch");
+  return NX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// general (unfused) pipeline for (m, R) without a fused instantiation: the
+// reference's own sequence CR(m) -> RobX -> CR(2m) x 2 -> RGC, one frame at a
+// time, reading only what the reference reads.
+// ---------------------------------------------------------------------------
+static size_t generic_frame_floats(const nx_esrrf_plan* p) {
+  const size_t planeM = (size_t)p->rowsM * p->colsM;
+  const size_t plane = (size_t)p->H * p->W;
+  return planeM /*mag*/ + 2 * plane /*gc, gr*/ + 2 * 4 * planeM /*gci, gri*/ + planeM /*rgc*/ +
+         2 * 64 /*shift arrays*/;
+}
+
+static int generic_frame(const nx_esrrf_plan* p, const float* frame, float* out_frame,
+                         float* scratch, cudaStream_t s) {
+  const size_t planeM = (size_t)p->rowsM * p->colsM;
+  const size_t plane = (size_t)p->H * p->W;
+  float* mag = scratch;
+  float* gc = mag + planeM;
+  float* gr = gc + plane;
+  float* gci = gr + plane;
+  float* gri = gci + 4 * planeM;
+  float* zeros = gri + 4 * planeM + planeM;
+  cudaError_t e = cudaMemsetAsync(zeros, 0, 64 * sizeof(float), s);
+  if (e != cudaSuccess) return cuda_status(e, "memset");
+  const int M = p->M;
+  e = launch_cr_shift_magnify(frame, 1, p->H, p->W, zeros, zeros, (float)M, (float)M, p->rowsM,
+                              p->colsM, mag, s);
+  if (e == cudaSuccess) e = launch_roberts_cross(frame, 1, p->H, p->W, gc, gr, s);
+  if (e == cudaSuccess)
+    e = launch_cr_shift_magnify(gc, 1, p->H, p->W, zeros, zeros, (float)(2 * M), (float)(2 * M),
+                                2 * p->rowsM, 2 * p->colsM, gci, s);
+  if (e == cudaSuccess)
+    e = launch_cr_shift_magnify(gr, 1, p->H, p->W, zeros, zeros, (float)(2 * M), (float)(2 * M),
+                                2 * p->rowsM, 2 * p->colsM, gri, s);
+  if (e == cudaSuccess)
+    e = launch_rgc(gci, gri, mag, 1, p->rowsM, p->colsM, M, p->sc, p->iw, out_frame, s);
+  if (e != cudaSuccess) return cuda_status(e, "unfused eSRRF frame");
+  return NX_OK;
+}
+
+}  // namespace nx
+
+using namespace nx;
+
+extern "C" {
+
+int nx_abi_version(void) { return NX_ABI_VERSION; }
+
+const char* nx_last_error(void) { return g_err; }
+
+int nx_esrrf_plan_create(nx_esrrf_plan** out, int H, int W, int magnification, float radius,
+                         float sensitivity, int do_intensity_weighting) {
+  if (!out) return invalid("plan out-pointer is NULL");
+  *out = nullptr;
+  if (H < 1 || W < 1) return invalid("image must have H, W >= 1");
+  if (magnification < 1 || magnification > 64) return invalid("magnification must be in [1, 64]");
+  if (!(radius > 0.f) || !(radius < 64.f)) return invalid("radius must be in (0, 64)");
+  if ((long long)H * magnification * 2 >= (1LL << 24) || (long long)W * magnification * 2 >= (1LL << 24))
+    return invalid("magnified image too large for float32 coordinates");
+  nx_esrrf_plan* p = new nx_esrrf_plan();
+  p->H = H;
+  p->W = W;
+  p->M = magnification;
+  p->radius = radius;
+  p->sensitivity = sensitivity;
+  p->iw = do_intensity_weighting ? 1 : 0;
+  p->rowsM = H * magnification;
+  p->colsM = W * magnification;
+  p->sc = rgc_scalars(magnification, radius, sensitivity, 0);
+  p->JW = std::max(-p->sc.start, p->sc.end - 1);
+  p->fused = (p->JW >= 1 && p->JW <= 6) ? fused_entry(magnification, p->JW) : nullptr;
+  clamp_taps(H, magnification, &p->cy_base, p->cy);
+  clamp_taps(W, magnification, &p->cx_base, p->cx);
+  cudaGetDevice(&p->device);
+  p->d_tbl = nullptr;
+  if (p->fused) {
+    std::vector<float> tbl, inv, wfull;
+    build_tables(p, tbl, inv, wfull);
+    p->n_tbl = tbl.size();
+    p->n_inv = inv.size();
+    p->n_wfull = wfull.size();
+    std::vector<float> all;
+    all.reserve(tbl.size() + inv.size() + wfull.size());
+    all.insert(all.end(), tbl.begin(), tbl.end());
+    all.insert(all.end(), inv.begin(), inv.end());
+    all.insert(all.end(), wfull.begin(), wfull.end());
+    cudaError_t e = cudaMalloc(&p->d_tbl, all.size() * sizeof(float));
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_status(e, "plan table allocation");
+    }
+    e = cudaMemcpy(p->d_tbl, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(p->d_tbl);
+      delete p;
+      return cuda_status(e, "plan table upload");
+    }
+  }
+  *out = p;
+  return NX_OK;
+}
+
+int nx_esrrf_weight_table(int magnification, float radius, float* h_out, size_t cap) {
+  if (magnification < 1 || magnification > 64) return invalid("magnification must be in [1, 64]");
+  if (!(radius > 0.f) || !(radius < 64.f)) return invalid("radius must be in (0, 64)");
+  nx_esrrf_plan tmp{};
+  tmp.M = magnification;
+  tmp.radius = radius;
+  tmp.sc = rgc_scalars(magnification, radius, 1.f, 0);
+  tmp.JW = std::max(-tmp.sc.start, tmp.sc.end - 1);
+  const size_t W2 = 2 * (size_t)tmp.JW + 1;
+  const size_t need = (size_t)magnification * magnification * W2 * W2;
+  if (h_out && cap >= need) {
+    std::vector<float> tbl, inv, wfull;
+    build_tables(&tmp, tbl, inv, wfull);
+    std::memcpy(h_out, wfull.data(), need * sizeof(float));
+  }
+  return tmp.JW;
+}
+
+int nx_esrrf_plan_destroy(nx_esrrf_plan* p) {
+  if (!p) return NX_OK;
+  if (p->d_tbl) cudaFree(p->d_tbl);
+  delete p;
+  return NX_OK;
+}
+
+size_t nx_esrrf_st_workspace_bytes(const nx_esrrf_plan* p, int T) {
+  (void)T;
+  if (!p) return 0;
+  size_t b = kStatusBytes;
+  if (!p->fused) b += align256(generic_frame_floats(p) * sizeof(float));
+  return b;
+}
+
+int nx_esrrf_st(const nx_esrrf_plan* p, const float* d_in, int T, float* d_out, void* d_ws,
+                size_t ws_bytes, void* stream) {
+  int rc = check_plan(p);
+  if (rc) return rc;
+  if (T < 0) return invalid("T must be >= 0");
+  if (T == 0) return NX_OK;
+  if (!d_in || !d_out) return invalid("NULL input/output");
+  if (!d_ws || ws_bytes < nx_esrrf_st_workspace_bytes(p, T)) {
+    set_error("workspace too small: need %zu bytes", nx_esrrf_st_workspace_bytes(p, T));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned* status = (unsigned*)d_ws;
+  NX_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
+  if (p->fused) return launch_fused_mode(p, kModeStack, d_in, T, T, 1, 1, d_out, status, s);
+  float* scratch = (float*)((char*)d_ws + kStatusBytes);
+  const size_t planeM = (size_t)p->rowsM * p->colsM;
+  for (int t = 0; t < T; ++t) {
+    rc = generic_frame(p, d_in + (size_t)t * p->H * p->W, d_out + (size_t)t * planeM, scratch, s);
+    if (rc) return rc;
+  }
+  return NX_OK;
+}
+
+size_t nx_esrrf_workspace_bytes(const nx_esrrf_plan* p, int T, int fpt, int corr_mask) {
+  if (!p || T < 1) return kStatusBytes;
+  if (fpt <= 0 || fpt > T) fpt = T;
+  const int n_tp = (T + fpt - 1) / fpt;
+  const size_t planeM = (size_t)p->rowsM * p->colsM;
+  const int F = fields_for(corr_mask);
+  size_t b = kStatusBytes;
+  if (p->fused) {
+    const int chunks = plan_chunks(p, T, fpt, n_tp);
+    b += align256((size_t)n_tp * chunks * F * planeM * sizeof(float));
+  } else {
+    b += align256((size_t)n_tp * 5 * planeM * sizeof(float));
+    b += align256(generic_frame_floats(p) * sizeof(float));
+  }
+  b += align256((size_t)corr_count(corr_mask) * n_tp * p->M * p->M * sizeof(float));
+  return b;
+}
+
+static int esrrf_validate(const nx_esrrf_plan* p, int T, int& fpt, int corr_mask, void* d_ws,
+                          size_t ws_bytes) {
+  int rc = check_plan(p);
+  if (rc) return rc;
+  if (T < 1) return invalid("need at least one frame");
+  if (corr_mask <= 0 || corr_mask > 7) return invalid("Type of correlation must be AVG, VAR or TAC2");
+  if (fpt <= 0 || fpt > T) fpt = T;
+  const size_t need = nx_esrrf_workspace_bytes(p, T, fpt, corr_mask);
+  if (!d_ws || ws_bytes < need) {
+    set_error("workspace too small: need %zu bytes", need);
+    return NX_ERR_WORKSPACE;
+  }
+  return NX_OK;
+}
+
+int nx_esrrf_run_stage1(const nx_esrrf_plan* p, const float* d_in, int T, int fpt, int corr_mask,
+                        void* d_ws, size_t ws_bytes, void* stream) {
+  int rc = esrrf_validate(p, T, fpt, corr_mask, d_ws, ws_bytes);
+  if (rc) return rc;
+  if (!d_in) return invalid("NULL input");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n_tp = (T + fpt - 1) / fpt;
+  const long long planeM = (long long)p->rowsM * p->colsM;
+  const int F = fields_for(corr_mask);
+  unsigned* status = (unsigned*)d_ws;
+  char* cur = (char*)d_ws + kStatusBytes;
+  NX_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
+  float* rec = (float*)cur;
+  if (p->fused) {
+    const int chunks = plan_chunks(p, T, fpt, n_tp);
+    return launch_fused_mode(p, F == 5 ? kModeFull : kModeSum, d_in, T, fpt, n_tp, chunks, rec,
+                             status, s);
+  }
+  cur += align256((size_t)n_tp * 5 * planeM * sizeof(float));
+  float* scratch = (float*)cur;
+  float* rgc_frame = scratch + (size_t)planeM + 2 * (size_t)p->H * p->W + 8 * (size_t)planeM;
+  for (int t = 0; t < T; ++t) {
+    const int tp = t / fpt;
+    rc = generic_frame(p, d_in + (size_t)t * p->H * p->W, rgc_frame, scratch, s);
+    if (rc) return rc;
+    cudaError_t e = launch_record_push_frame(rgc_frame, planeM, rec + (size_t)tp * 5 * planeM,
+                                             t - tp * fpt, s);
+    if (e != cudaSuccess) return cuda_status(e, "record push");
+  }
+  return NX_OK;
+}
+
+int nx_esrrf_run_stage2(const nx_esrrf_plan* p, int T, int fpt, int corr_mask, int mpc,
+                        float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+  int rc = esrrf_validate(p, T, fpt, corr_mask, d_ws, ws_bytes);
+  if (rc) return rc;
+  if (!d_out) return invalid("NULL output");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n_tp = (T + fpt - 1) / fpt;
+  const long long planeM = (long long)p->rowsM * p->colsM;
+  const int F = fields_for(corr_mask);
+  const int ncorr = corr_count(corr_mask);
+  char* cur = (char*)d_ws + kStatusBytes;
+  float* rec = (float*)cur;
+  int chunks = 1, Fr = 5;
+  if (p->fused) {
+    chunks = plan_chunks(p, T, fpt, n_tp);
+    Fr = F;
+    cur += align256((size_t)n_tp * chunks * F * planeM * sizeof(float));
+  } else {
+    cur += align256((size_t)n_tp * 5 * planeM * sizeof(float));
+    cur += align256(generic_frame_floats(p) * sizeof(float));
+  }
+  float* map = (float*)cur;
+  for (int tp = 0; tp < n_tp; ++tp) {
+    const int nf = std::min(fpt, T - tp * fpt);
+    const int nch = std::min(chunks, nf);
+    cudaError_t e = launch_finalize(rec + (size_t)tp * chunks * Fr * planeM, Fr, nch, nf, planeM,
+                                    corr_mask, d_out + (size_t)tp * planeM,
+                                    (long long)n_tp * planeM, s);
+    if (e != cudaSuccess) return cuda_status(e, "temporal finalize");
+  }
+  if (mpc) {
+    cudaError_t e = launch_mpc(d_out, ncorr * n_tp, p->rowsM, p->colsM, p->M, map, s);
+    if (e != cudaSuccess) return cuda_status(e, "macro-pixel correction");
+  }
+  return NX_OK;
+}
+
+int nx_esrrf_run(const nx_esrrf_plan* p, const float* d_in, int T, int fpt, int corr_mask,
+                 int mpc, float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+  if (!d_out) return invalid("NULL output");
+  int rc = nx_esrrf_run_stage1(p, d_in, T, fpt, corr_mask, d_ws, ws_bytes, stream);
+  if (rc) return rc;
+  return nx_esrrf_run_stage2(p, T, fpt, corr_mask, mpc, d_out, d_ws, ws_bytes, stream);
+}
+
+size_t nx_esrrf_accum_bytes(const nx_esrrf_plan* p) {
+  if (!p) return 0;
+  return align256((size_t)5 * p->rowsM * p->colsM * sizeof(float));
+}
+
+size_t nx_esrrf_push_workspace_bytes(const nx_esrrf_plan* p, int T_block) {
+  if (!p || T_block < 1) return kStatusBytes;
+  return nx_esrrf_workspace_bytes(p, T_block, T_block, NX_CORR_VAR | NX_CORR_TAC2);
+}
+
+int nx_esrrf_accum_push(const nx_esrrf_plan* p, const float* d_block, int T_block,
+                        int frames_before, void* d_accum, void* d_ws, size_t ws_bytes,
+                        void* stream) {
+  int rc = check_plan(p);
+  if (rc) return rc;
+  if (T_block < 1 || frames_before < 0) return invalid("bad block size / frame offset");
+  if (!d_block || !d_accum) return invalid("NULL block/accumulator");
+  const size_t need = nx_esrrf_push_workspace_bytes(p, T_block);
+  if (!d_ws || ws_bytes < need) {
+    set_error("workspace too small: need %zu bytes", need);
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long planeM = (long long)p->rowsM * p->colsM;
+  unsigned* status = (unsigned*)d_ws;
+  float* rec = (float*)((char*)d_ws + kStatusBytes);
+  float* acc = (float*)d_accum;
+  // block records: chunks merged in order into rec chunk 0 ... then into acc
+  int chunks = 1;
+  if (p->fused) {
+    chunks = plan_chunks(p, T_block, T_block, 1);
+    rc = launch_fused_mode(p, kModeFull, d_block, T_block, T_block, 1, chunks, rec, status, s);
+    if (rc) return rc;
+  } else {
+    float* scratch = rec + align256((size_t)5 * planeM * sizeof(float)) / sizeof(float);
+    float* rgc_frame = scratch + (size_t)planeM + 2 * (size_t)p->H * p->W + 8 * (size_t)planeM;
+    for (int t = 0; t < T_block; ++t) {
+      rc = generic_frame(p, d_block + (size_t)t * p->H * p->W, rgc_frame, scratch, s);
+      if (rc) return rc;
+      cudaError_t e = launch_record_push_frame(rgc_frame, planeM, rec, t, s);
+      if (e != cudaSuccess) return cuda_status(e, "record push");
+    }
+  }
+  int n_acc = frames_before;
+  for (int c = 0; c < chunks; ++c) {
+    const int nc = (int)((long long)(c + 1) * T_block / chunks - (long long)c * T_block / chunks);
+    cudaError_t e;
+    if (n_acc == 0) {
+      e = cudaMemcpyAsync(acc, rec + (size_t)c * 5 * planeM, (size_t)5 * planeM * sizeof(float),
+                          cudaMemcpyDeviceToDevice, s);
+    } else {
+      e = launch_record_merge(acc, rec + (size_t)c * 5 * planeM, planeM, n_acc, nc, s);
+    }
+    if (e != cudaSuccess) return cuda_status(e, "accumulator merge");
+    n_acc += nc;
+  }
+  return NX_OK;
+}
+
+int nx_esrrf_accum_finalize(const nx_esrrf_plan* p, const void* d_accum, int total_frames,
+                            int corr_mask, int mpc, float* d_out, void* d_ws, size_t ws_bytes,
+                            void* stream) {
+  int rc = check_plan(p);
+  if (rc) return rc;
+  if (total_frames < 1) return invalid("no frames were pushed");
+  if (corr_mask <= 0 || corr_mask > 7) return invalid("Type of correlation must be AVG, VAR or TAC2");
+  const int ncorr = corr_count(corr_mask);
+  const size_t need = kStatusBytes + align256((size_t)ncorr * p->M * p->M * sizeof(float));
+  if (!d_ws || ws_bytes < need) {
+    set_error("workspace too small: need %zu bytes", need);
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long planeM = (long long)p->rowsM * p->colsM;
+  cudaError_t e = launch_finalize((const float*)d_accum, 5, 1, total_frames, planeM, corr_mask,
+                                  d_out, planeM, s);
+  if (e != cudaSuccess) return cuda_status(e, "temporal finalize");
+  if (mpc) {
+    float* map = (float*)((char*)d_ws + kStatusBytes);
+    e = launch_mpc(d_out, ncorr, p->rowsM, p->colsM, p->M, map, s);
+    if (e != cudaSuccess) return cuda_status(e, "macro-pixel correction");
+  }
+  return NX_OK;
+}
+
+int nx_workspace_status(const void* d_ws, void* stream) {
+  if (!d_ws) return invalid("NULL workspace");
+  unsigned st = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  NX_CUDA_TRY(cudaMemcpyAsync(&st, d_ws, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  NX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (st & kDevTmaTimeout) {
+    set_error("a TMA tile wait timed out on the device (status 0x%x)", st);
+    return NX_ERR_DEVICE_TIMEOUT;
+  }
+  if (st) {
+    set_error("device status 0x%x", st);
+    return NX_ERR_CUDA;
+  }
+  return NX_OK;
+}
+
+int nx_cr_shift_magnify(const float* d_in, int T, int H, int W, const float* d_shift_row,
+                        const float* d_shift_col, float mag_row, float mag_col, float* d_out,
+                        void* stream) {
+  if (T < 0 || H < 1 || W < 1) return invalid("bad image shape");
+  if (!(mag_row > 0.f) || !(mag_col > 0.f)) return invalid("magnification must be > 0");
+  const int rowsM = (int)((float)H * mag_row);
+  const int colsM = (int)((float)W * mag_col);
+  cudaError_t e = launch_cr_shift_magnify(d_in, T, H, W, d_shift_row, d_shift_col, mag_row,
+                                          mag_col, rowsM, colsM, d_out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "ShiftAndMagnify");
+  return NX_OK;
+}
+
+int nx_roberts_cross(const float* d_in, int T, int H, int W, float* d_gc, float* d_gr,
+                     void* stream) {
+  if (T < 0 || H < 1 || W < 1) return invalid("bad image shape");
+  cudaError_t e = launch_roberts_cross(d_in, T, H, W, d_gc, d_gr, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "GradientRobertsCross");
+  return NX_OK;
+}
+
+int nx_rgc(const float* d_gc, const float* d_gr, const float* d_img, int T, int rowsM, int colsM,
+           int magnification, float radius, float sensitivity, int iw, int pad_edges,
+           float* d_out, void* stream) {
+  if (T < 0 || rowsM < 1 || colsM < 1) return invalid("bad image shape");
+  if (magnification < 1) return invalid("magnification must be >= 1");
+  if (!(radius > 0.f)) return invalid("radius must be > 0");
+  const RgcScalars sc = rgc_scalars(magnification, radius, sensitivity, pad_edges);
+  cudaError_t e = launch_rgc(d_gc, d_gr, d_img, T, rowsM, colsM, magnification, sc, iw ? 1 : 0,
+                             d_out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "RadialGradientConvergence");
+  return NX_OK;
+}
+
+size_t nx_radiality_workspace_bytes(int T, int h, int w) {
+  return align256((size_t)2 * T * h * w * sizeof(float));
+}
+
+int nx_radiality(const float* d_img, const float* d_img_interp, int T, int h, int w,
+                 int magnification, float ring_radius, int border, int positivity, int iw,
+                 float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+  if (T < 0 || h < 1 || w < 1) return invalid("bad image shape");
+  if (magnification < 1) return invalid("magnification must be >= 1");
+  if (!d_ws || ws_bytes < nx_radiality_workspace_bytes(T, h, w)) {
+    set_error("workspace too small: need %zu bytes", nx_radiality_workspace_bytes(T, h, w));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  float* gx = (float*)d_ws;
+  float* gy = gx + (size_t)T * h * w;
+  cudaError_t e = launch_gradient_radiality(d_img, T, h, w, gx, gy, s);
+  if (e == cudaSuccess)
+    e = launch_radiality(gx, gy, d_img_interp, T, h, w, magnification,
+                         ring_coords(magnification, ring_radius), border, positivity ? 1 : 0,
+                         iw ? 1 : 0, d_out, s);
+  if (e != cudaSuccess) return cuda_status(e, "Radiality");
+  return NX_OK;
+}
+
+int nx_temporal_correlation(const float* d_stack, int T, long long n, int corr, float* d_out,
+                            void* stream) {
+  if (T < 1 || n < 0) return invalid("bad stack shape");
+  if (corr != NX_CORR_AVG && corr != NX_CORR_VAR && corr != NX_CORR_TAC2)
+    return invalid("Type of correlation must be AVG, VAR or TAC2");
+  cudaError_t e = launch_temporal_stack(d_stack, T, n, corr, d_out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "temporal correlation");
+  return NX_OK;
+}
+
+int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n, int order,
+                                 float* d_out, void* stream) {
+  if (T < 1 || n < 0) return invalid("bad stack shape");
+  if (order > 4 || order < -1) return invalid("order must be -1, 0, 1, 2, 3 or 4");
+  cudaError_t e = launch_srrf_temporal(d_stack, T, n, order, d_out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "SRRF temporal correlation");
+  return NX_OK;
+}
+
+size_t nx_macro_pixel_workspace_bytes(int S, int magnification) {
+  return align256((size_t)std::max(S, 1) * magnification * magnification * sizeof(float));
+}
+
+int nx_macro_pixel_correct(float* d_img, int S, int rowsM, int colsM, int magnification,
+                           void* d_ws, size_t ws_bytes, void* stream) {
+  if (S < 0 || rowsM < 0 || colsM < 0) return invalid("bad image shape");
+  if (magnification < 1) return invalid("magnification must be >= 1");
+  if (!d_ws || ws_bytes < nx_macro_pixel_workspace_bytes(S, magnification)) {
+    set_error("workspace too small");
+    return NX_ERR_WORKSPACE;
+  }
+  cudaError_t e = launch_mpc(d_img, S, rowsM, colsM, magnification, (float*)d_ws,
+                             (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "macro-pixel correction");
+  return NX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// Shared device/host helpers for the eSRRF/SRRF engine (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "nanopyx_gb300.h"
+
+namespace nx {
+
+// ---------------------------------------------------------------------------
+// status words written by kernels (device) and returned by the C-ABI (host)
+// ---------------------------------------------------------------------------
+enum DeviceStatusBits : unsigned {
+  kDevOk = 0u,
+  kDevTmaTimeout = 1u << 0,   // an mbarrier wait for a TMA tile ran out of time
+  kDevBadGeometry = 1u << 1,  // a launch saw an impossible tile geometry
+};
+
+// Bounded-wait budget for every device spin (ns of %globaltimer).
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier + TMA (cp.async.bulk.tensor) wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for phase `parity` of `bar`; gives up after kWaitLimitNs and returns false.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+// 3-D tiled TMA load (x fastest).  The x coordinate must be a multiple of 4
+// floats (16 B); callers guarantee it by construction.
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, uint64_t* bar, int x, int y,
+                                            int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cta.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Catmull-Rom (Keys, a = 0.5) weight of one tap, float arithmetic.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ float cr_cubic(float v) {
+  v = fabsf(v);
+  if (v < 1.f) return v * v * (1.5f * v - 2.5f) + 1.f;
+  if (v < 2.f) return ((-0.5f * v + 2.5f) * v - 4.f) * v + 2.f;
+  return 0.f;
+}
+
+__host__ __device__ __forceinline__ int floordiv(int a, int b) {
+  int q = a / b;
+  return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
+}
+
+}  // namespace nx
+
+// host-side error plumbing shared by the C-ABI translation units
+namespace nx {
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+}  // namespace nx
+
+#define NX_CUDA_TRY(call)                                            \
+  do {                                                               \
+    cudaError_t _e = (call);                                         \
+    if (_e != cudaSuccess) return ::nx::cuda_status(_e, #call);      \
+  } while (0)

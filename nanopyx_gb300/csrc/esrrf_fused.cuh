@@ -1,0 +1,543 @@
+// Fused eSRRF frame-loop kernel (sm_103a).
+//
+// One CTA owns a 32 x TY tile of input pixels (= a 32M x TY*M tile of output
+// pixels), one timepoint and one contiguous chunk of that timepoint's frames.
+// Per frame it
+//   1. receives the input tile + halo by TMA (double-buffered, mbarrier), or
+//      by plain loads when the row pitch is not 16-byte aligned;
+//   2. computes Roberts-Cross gradients          (_c_gradients.c:53-73);
+//   3. Catmull-Rom-interpolates them on the half-pixel grid -- the only
+//      positions the reference RGC ever reads from its 2m-magnified gradient
+//      images (rows/cols k*m, clamped to 2*m*H-1;
+//      _c_sr_radial_gradient_convergence.c:45-61) -- and normalises them;
+//   4. Catmull-Rom-magnifies the intensity       (_c_interpolation_catmull_rom.c:21-52);
+//   5. evaluates RGC for its M output pixels per thread with FP64-derived
+//      phase tables of the distance weights      (_c_sr_radial_gradient_convergence.c:17-90);
+//   6. applies ^sensitivity, intensity weighting and the margin, and either
+//      writes the per-frame value (eSRRF_ST stack) or folds it into per-pixel
+//      temporal sums kept in registers (shift K = first value; S, Q, P, L).
+// Nothing of size (T, 2Hm, 2Wm) or (T, Hm, Wm) is ever materialised for the
+// temporal modes.
+#pragma once
+
+#include <cuda.h>
+
+#include "common.cuh"
+
+namespace nx {
+
+enum FusedMode : int { kModeStack = 0, kModeSum = 1, kModeFull = 2 };
+
+__host__ __device__ constexpr int mode_fields(int mode) {
+  return mode == kModeFull ? 5 : (mode == kModeSum ? 2 : 0);
+}
+
+struct FusedParams {
+  const float* in;     // (T, H, W)
+  int T, H, W;
+  int rowsM, colsM;
+  int tiles_x;
+  int fpt;             // frames per timepoint
+  int n_tp;            // number of timepoints
+  int chunks;          // chunks per timepoint (the last timepoint uses min(chunks, its frames))
+  int margin;
+  int iw;
+  int sens_mode;       // 0: none, 1: integer power sens_int, 2: powf(sens)
+  int sens_int;
+  float sens;
+  int cy_base, cx_base;  // first tap row/col of the clamped half-grid index 2H / 2W
+  float cy[4], cx[4];
+  const float* tbl;      // [M][2J+1][3][NS4*4]  (a = dx*w/d, b = dy*w/d, w) per sample
+  const float* inv_wsum; // [M][M]
+  const float* wfull;    // [M][M][2J+1][2J+1]
+  float* out;            // stack (T, rowsM, colsM) or records [n_tp*chunks][F][rowsM][colsM]
+  unsigned* status;
+  int use_tma;
+};
+
+template <int M>
+struct TileRows {
+  // input-pixel rows per CTA tile: keeps 32*TY*M threads <= 640
+  static constexpr int TY = (M <= 2) ? 8 : (M <= 4 ? 4 : 2);
+};
+
+template <int M, int J, int TY>
+struct Geo {
+  static constexpr int TX = 32;
+  static constexpr int W2 = 2 * J + 1;
+  static constexpr int NQ = 2 * J + 2;
+  static constexpr int HG_R = 2 * TY + 2 * J;
+  static constexpr int HG_C = 2 * TX + 2 * J;
+  static constexpr int HGP = TX + J;
+  static constexpr int RLO = (J + 1) / 2 + 2;
+  static constexpr int RHI = TY + (J - 1) / 2 + 2;
+  static constexpr int NRY = RLO + RHI;
+  static constexpr int CLO = (J + 1) / 2 + 2;
+  static constexpr int CHI = TX + (J - 1) / 2 + 2;
+  static constexpr int NCX = CLO + CHI;
+  static constexpr int IY = RLO + 1;
+  static constexpr int BH = NRY + 1;
+  static constexpr int IX = ((CLO + 1 + 3) / 4) * 4;
+  static constexpr int BW = ((IX + CHI + 3) / 4) * 4;
+  static constexpr int NS = M * W2;
+  static constexpr int NS4 = (NS + 3) / 4;
+  static constexpr int OY = TY * M;
+  static constexpr int OX = TX * M;
+  static constexpr int RIW = TX + 4;
+  static constexpr int NT = 32 * TY * M;
+
+  static constexpr int al(int n) { return (n + 31) / 32 * 32; }
+  // shared-memory layout (in floats, 128-byte aligned blocks)
+  static constexpr int O_INB = 0;
+  static constexpr int S_INB = al(BH * BW);
+  static constexpr int O_G = O_INB + 2 * S_INB;
+  static constexpr int S_G = al(NRY * NCX);
+  static constexpr int O_T1 = O_G + 2 * S_G;
+  static constexpr int S_T1 = al(NRY * HG_C);
+  static constexpr int O_HG = O_T1 + 2 * S_T1;
+  static constexpr int S_HG = al(HG_R * 2 * HGP * 2);
+  static constexpr int O_RI = O_HG + S_HG;
+  static constexpr int S_RI = al(OY * RIW);
+  static constexpr int O_IN = O_RI + S_RI;
+  static constexpr int S_IN = al(OY * OX);
+  static constexpr int O_TB = O_IN + S_IN;
+  static constexpr int S_TB = al(M * W2 * 3 * NS4 * 4);
+  static constexpr int O_RW = O_TB + S_TB;
+  static constexpr int S_RW = al(OY * 5);
+  static constexpr int O_CW = O_RW + S_RW;
+  static constexpr int S_CW = al(OX * 5);
+  static constexpr int O_BAR = O_CW + S_CW;
+  static constexpr int FLOATS = O_BAR + 32;
+  static constexpr size_t SMEM_BYTES = size_t(FLOATS) * 4;
+};
+
+__device__ __forceinline__ float f4c(const float4& v, int e) {
+  return e == 0 ? v.x : (e == 1 ? v.y : (e == 2 ? v.z : v.w));
+}
+
+template <int M, int J, int TY, int MODE>
+__global__ void __launch_bounds__(32 * TY * M, 1)
+    esrrf_fused_kernel(const __grid_constant__ CUtensorMap tmap, const FusedParams p) {
+  using G = Geo<M, J, TY>;
+  constexpr int F = mode_fields(MODE);
+  extern __shared__ __align__(128) float sm[];
+  float* inb = sm + G::O_INB;
+  float* gsm = sm + G::O_G;
+  float* t1 = sm + G::O_T1;
+  float2* hg = reinterpret_cast<float2*>(sm + G::O_HG);
+  float* ri = sm + G::O_RI;
+  float* inten = sm + G::O_IN;
+  float4* tb4 = reinterpret_cast<float4*>(sm + G::O_TB);
+  float* rw = sm + G::O_RW;
+  float* cw = sm + G::O_CW;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + G::O_BAR);
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int ty = warp % TY;
+  const int py = warp / TY;
+
+  const int tile = blockIdx.x;
+  const int tile_x = tile % p.tiles_x;
+  const int tile_y = tile / p.tiles_x;
+  const int nx0 = tile_x * G::TX;
+  const int ny0 = tile_y * TY;
+  const int tp = blockIdx.y / p.chunks;
+  const int chunk = blockIdx.y % p.chunks;
+  const int H = p.H, W = p.W;
+
+  // frames of this CTA
+  const int tp_f0 = tp * p.fpt;
+  const int tp_nf = min(p.fpt, p.T - tp_f0);
+  const int nch = min(p.chunks, tp_nf);
+  if (chunk >= nch) return;  // uniform across the CTA
+  const int f0 = tp_f0 + (int)((long long)chunk * tp_nf / nch);
+  const int f1 = tp_f0 + (int)((long long)(chunk + 1) * tp_nf / nch);
+
+  const int kb_y = 2 * ny0 - J;
+  const int kb_x = 2 * nx0 - J;
+  const int RY0 = ny0 - G::RLO;
+  const int CX0 = nx0 - G::CLO;
+  const int y_start = ny0 - G::IY;
+  const int x_start = nx0 - G::IX;
+  const int twoH = 2 * H, twoW = 2 * W;
+  const int kmax_y = 2 * p.rowsM - 2, kmax_x = 2 * p.colsM - 2;
+
+  // ---- per-CTA constants: RGC tables, intensity weights ------------------
+  {
+    const float4* src = reinterpret_cast<const float4*>(p.tbl);
+    for (int i = tid; i < M * G::W2 * 3 * G::NS4; i += G::NT) tb4[i] = src[i];
+    for (int i = tid; i < G::OY; i += G::NT) {
+      const int yM = ny0 * M + i;
+      const int ny = ny0 + i / M;
+      const float ry = __fdiv_rn((float)yM, (float)M);
+      const int rb = (int)floorf(ry - 0.5f);
+      float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int nb = rb - 1 + t;
+        const int k = nb - (ny - 2);
+        const float w = cr_cubic(ry - ((float)nb + 0.5f));
+#pragma unroll
+        for (int kk = 0; kk < 5; ++kk) w5[kk] = (k == kk) ? w : w5[kk];
+      }
+#pragma unroll
+      for (int k = 0; k < 5; ++k) rw[i * 5 + k] = w5[k];
+    }
+    for (int i = tid; i < G::OX; i += G::NT) {
+      const int xM = nx0 * M + i;
+      const int nxp = nx0 + i / M;
+      const float rx = __fdiv_rn((float)xM, (float)M);
+      const int cb = (int)floorf(rx - 0.5f);
+      float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int nb = cb - 1 + t;
+        const int k = nb - (nxp - 2);
+        const float w = cr_cubic(rx - ((float)nb + 0.5f));
+#pragma unroll
+        for (int kk = 0; kk < 5; ++kk) w5[kk] = (k == kk) ? w : w5[kk];
+      }
+#pragma unroll
+      for (int k = 0; k < 5; ++k) cw[i * 5 + k] = w5[k];
+    }
+  }
+
+  // ---- per-thread constants ------------------------------------------------
+  const int ny = ny0 + ty;
+  const int nx = nx0 + lane;
+  const int yM = ny * M + py;
+  const int cpy = (2 * py + 1) / M;
+  float inv_w[M];
+  unsigned omask = 0;  // bit px: output forced to 0 / not written
+  {
+    const int ky_lo = 2 * ny + cpy - J, ky_hi = 2 * ny + cpy + J;
+    const bool by = (ky_lo < 1) || (ky_hi > kmax_y);
+#pragma unroll
+    for (int px = 0; px < M; ++px) {
+      const int cpx = (2 * px + 1) / M;
+      const int xM = nx * M + px;
+      const int kx_lo = 2 * nx + cpx - J, kx_hi = 2 * nx + cpx + J;
+      float iw = p.inv_wsum[py * M + px];
+      if (by || kx_lo < 1 || kx_hi > kmax_x) {
+        // window reaches invalid half-grid samples: they count in neither sum
+        const float* wf = p.wfull + (size_t)(py * M + px) * G::W2 * G::W2;
+        float s = 0.f;
+        for (int jj = 0; jj < G::W2; ++jj) {
+          const int ky = ky_lo + jj;
+          if (ky < 1 || ky > kmax_y) continue;
+          for (int ii = 0; ii < G::W2; ++ii) {
+            const int kx = kx_lo + ii;
+            if (kx < 1 || kx > kmax_x) continue;
+            s += wf[jj * G::W2 + ii];
+          }
+        }
+        iw = s > 0.f ? 1.f / s : 0.f;
+      }
+      inv_w[px] = iw;
+      const bool outside = (ny >= H) || (nx >= W);
+      const bool in_margin = (yM < p.margin) || (yM >= p.rowsM - p.margin) ||
+                             (xM < p.margin) || (xM >= p.colsM - p.margin);
+      if (outside) omask |= (1u << px) | (1u << 31);
+      else if (in_margin) omask |= (1u << px);
+    }
+  }
+
+  float accK[M], accS[M], accQ[M], accP[M], accL[M];
+#pragma unroll
+  for (int px = 0; px < M; ++px) {
+    accK[px] = 0.f; accS[px] = 0.f; accQ[px] = 0.f; accP[px] = 0.f; accL[px] = 0.f;
+  }
+
+  constexpr unsigned kTileBytes = unsigned(G::BH * G::BW * 4);
+  const bool use_tma = p.use_tma != 0;
+  if (use_tma) {
+    if (tid == 0) {
+      mbar_init(&bar[0], 1);
+      mbar_init(&bar[1], 1);
+      fence_mbar_init();
+    }
+  }
+  __syncthreads();
+  if (use_tma && tid == 0) {
+    for (int k = 0; k < 2; ++k) {
+      if (f0 + k < f1) {
+        mbar_arrive_expect_tx(&bar[k], kTileBytes);
+        tma_load_3d(inb + k * G::S_INB, &tmap, &bar[k], x_start, y_start, f0 + k);
+      }
+    }
+  }
+
+  const size_t plane = (size_t)p.rowsM * p.colsM;
+  int abort_it = -1;
+
+  for (int f = f0; f < f1; ++f) {
+    const int it = f - f0;
+    const int b = it & 1;
+    float* tin = inb + b * G::S_INB;
+    if (use_tma) {
+      const bool ok = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) & 1));
+      if (__syncthreads_or(!ok)) {
+        if (tid == 0) atomicOr(p.status, kDevTmaTimeout);
+        abort_it = it;
+        break;
+      }
+    } else {
+      const float* src = p.in + (size_t)f * H * W;
+      for (int i = tid; i < G::BH * G::BW; i += G::NT) {
+        const int r = y_start + i / G::BW;
+        const int c = x_start + i % G::BW;
+        tin[i] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(src + (size_t)r * W + c) : 0.f;
+      }
+      __syncthreads();
+    }
+
+    // ---- phase 1: Roberts-Cross, intensity row pass --------------------
+    for (int i = tid; i < G::NRY * G::NCX; i += G::NT) {
+      const int rl = i / G::NCX, cl = i % G::NCX;
+      const int r = RY0 + rl, c = CX0 + cl;
+      float gc = 0.f, gr = 0.f;
+      if (r >= 0 && r < H && c >= 0 && c < W) {
+        const int r0 = r > 0 ? r - 1 : 0;
+        const int c0 = c > 0 ? c - 1 : 0;
+        const float a = tin[(r0 - y_start) * G::BW + (c - x_start)];   // image[r0][c1]
+        const float bb = tin[(r - y_start) * G::BW + (c0 - x_start)];  // image[r1][c0]
+        const float d = tin[(r0 - y_start) * G::BW + (c0 - x_start)];  // image[r0][c0]
+        const float e = tin[(r - y_start) * G::BW + (c - x_start)];    // image[r1][c1]
+        gc = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
+        gr = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
+      }
+      gsm[i] = gc;
+      gsm[G::S_G + i] = gr;
+    }
+    for (int i = tid; i < G::OY * G::RIW; i += G::NT) {
+      const int oy = i / G::RIW, cc = i % G::RIW;
+      const int nyo = ny0 + oy / M;
+      const float* w5 = rw + oy * 5;
+      const float* col = tin + (nyo - 2 - y_start) * G::BW + (nx0 - 2 + cc - x_start);
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) s = fmaf(w5[k], col[k * G::BW], s);
+      ri[i] = s;
+    }
+    __syncthreads();
+    if (use_tma && tid == 0 && f + 2 < f1) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[b], kTileBytes);
+      tma_load_3d(tin, &tmap, &bar[b], x_start, y_start, f + 2);
+    }
+
+    // ---- phase 2: gradient column pass onto half-grid columns; intensity --
+    for (int i = tid; i < G::NRY * G::HG_C; i += G::NT) {
+      const int rl = i / G::HG_C, kxl = i % G::HG_C;
+      const int kx = kb_x + kxl;
+      float vc = 0.f, vr = 0.f;
+      if (kx >= 1 && kx <= kmax_x) {
+        const float* g0 = gsm + rl * G::NCX;
+        const float* g1 = gsm + G::S_G + rl * G::NCX;
+        if (kx >= twoW) {
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int cl = p.cx_base + t - CX0;
+            vc = fmaf(p.cx[t], g0[cl], vc);
+            vr = fmaf(p.cx[t], g1[cl], vr);
+          }
+        } else if (kx & 1) {
+          const int cl = ((kx - 1) >> 1) - CX0;
+          vc = g0[cl];
+          vr = g1[cl];
+        } else {
+          const int cl = (kx >> 1) - 2 - CX0;
+          vc = -0.0625f * g0[cl];
+          vr = -0.0625f * g1[cl];
+          vc = fmaf(0.5625f, g0[cl + 1], vc);
+          vr = fmaf(0.5625f, g1[cl + 1], vr);
+          vc = fmaf(0.5625f, g0[cl + 2], vc);
+          vr = fmaf(0.5625f, g1[cl + 2], vr);
+          vc = fmaf(-0.0625f, g0[cl + 3], vc);
+          vr = fmaf(-0.0625f, g1[cl + 3], vr);
+        }
+      }
+      t1[i] = vc;
+      t1[G::S_T1 + i] = vr;
+    }
+    for (int i = tid; i < G::OY * G::OX; i += G::NT) {
+      const int oy = i / G::OX, ox = i % G::OX;
+      const float* w5 = cw + ox * 5;
+      const float* rr = ri + oy * G::RIW + ox / M;
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < 5; ++k) s = fmaf(w5[k], rr[k], s);
+      inten[i] = s;
+    }
+    __syncthreads();
+
+    // ---- phase 3: gradient row pass, normalise -> half-grid tile ----------
+    for (int i = tid; i < G::HG_R * G::HG_C; i += G::NT) {
+      const int kyl = i / G::HG_C, kxl = i % G::HG_C;
+      const int ky = kb_y + kyl, kx = kb_x + kxl;
+      float2 n = make_float2(0.f, 0.f);
+      if (ky >= 1 && ky <= kmax_y && kx >= 1 && kx <= kmax_x) {
+        const float* c0 = t1 + kxl;
+        const float* c1 = t1 + G::S_T1 + kxl;
+        float gx = 0.f, gy = 0.f;
+        if (ky >= twoH) {
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            const int rl = p.cy_base + t - RY0;
+            gx = fmaf(p.cy[t], c0[rl * G::HG_C], gx);
+            gy = fmaf(p.cy[t], c1[rl * G::HG_C], gy);
+          }
+        } else if (ky & 1) {
+          const int rl = ((ky - 1) >> 1) - RY0;
+          gx = c0[rl * G::HG_C];
+          gy = c1[rl * G::HG_C];
+        } else {
+          const int rl = (ky >> 1) - 2 - RY0;
+          gx = -0.0625f * c0[rl * G::HG_C];
+          gy = -0.0625f * c1[rl * G::HG_C];
+          gx = fmaf(0.5625f, c0[(rl + 1) * G::HG_C], gx);
+          gy = fmaf(0.5625f, c1[(rl + 1) * G::HG_C], gy);
+          gx = fmaf(0.5625f, c0[(rl + 2) * G::HG_C], gx);
+          gy = fmaf(0.5625f, c1[(rl + 2) * G::HG_C], gy);
+          gx = fmaf(-0.0625f, c0[(rl + 3) * G::HG_C], gx);
+          gy = fmaf(-0.0625f, c1[(rl + 3) * G::HG_C], gy);
+        }
+        const float m2 = fmaf(gx, gx, gy * gy);
+        if (m2 > 0.f) {
+          const float inv = rsqrtf(m2);
+          n = make_float2(gx * inv, gy * inv);
+        }
+      }
+      hg[(kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1)] = n;
+    }
+    __syncthreads();
+
+    // ---- phase 4: RGC for this thread's M outputs --------------------------
+    float acc[M];
+#pragma unroll
+    for (int px = 0; px < M; ++px) acc[px] = 0.f;
+#pragma unroll
+    for (int jj = 0; jj < G::W2; ++jj) {
+      const int kyl = 2 * ty + cpy + jj;
+      const float2* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
+      const float2* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
+      float2 sv[G::NQ];
+#pragma unroll
+      for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
+      const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * 3 * G::NS4;
+#pragma unroll
+      for (int s4 = 0; s4 < G::NS4; ++s4) {
+        const float4 A = tb[s4];
+        const float4 B = tb[G::NS4 + s4];
+        const float4 Wv = tb[2 * G::NS4 + s4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int sidx = s4 * 4 + e;
+          if (sidx < G::NS) {
+            const int px = sidx / G::W2;
+            const int ii = sidx % G::W2;
+            const int cpx = (2 * px + 1) / M;
+            const float2 gv = sv[cpx + ii];
+            const float a = f4c(A, e), bb = f4c(B, e), w = f4c(Wv, e);
+            const float dp = fmaf(gv.x, a, gv.y * bb);
+            const float u = fmaf(gv.y, a, -(gv.x * bb));
+            const float v = w - fabsf(u);
+            acc[px] = (dp < 0.f) ? acc[px] + v : acc[px];
+          }
+        }
+      }
+    }
+
+    // ---- epilogue: normalise, ^sensitivity, intensity, margin, temporal ----
+    const float* irow = inten + (ty * M + py) * G::OX + lane * M;
+#pragma unroll
+    for (int px = 0; px < M; ++px) {
+      float r = acc[px] * inv_w[px];
+      r = (r < 0.f) ? 0.f : r;
+      if (p.sens_mode == 1) {
+        const float base = r;
+        for (int k = 1; k < p.sens_int; ++k) r *= base;
+      } else if (p.sens_mode == 2) {
+        r = powf(r, p.sens);
+      }
+      if (p.iw) r *= irow[px];
+      if (omask & (1u << px)) r = 0.f;
+      if (MODE == kModeStack) {
+        if (!(omask >> 31)) p.out[(size_t)f * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
+      } else {
+        if (it == 0) accK[px] = r;
+        const float y = r - accK[px];
+        accS[px] += y;
+        if (MODE == kModeFull) {
+          accQ[px] = fmaf(y, y, accQ[px]);
+          accP[px] = fmaf(accL[px], y, accP[px]);
+          accL[px] = y;
+        }
+      }
+    }
+  }
+
+  if (abort_it >= 0) {
+    // a TMA tile never arrived: wait (bounded) for the copies still in flight
+    // (this frame's and the next one's), then leave without writing
+    if (tid == 0) {
+      const int bb = abort_it & 1;
+      (void)mbar_wait_bounded(&bar[bb], (unsigned)((abort_it >> 1) & 1));
+      if (f0 + abort_it + 1 < f1)
+        (void)mbar_wait_bounded(&bar[bb ^ 1], (unsigned)(((abort_it + 1) >> 1) & 1));
+    }
+    return;
+  }
+
+  if (MODE != kModeStack && !(omask >> 31)) {
+    float* rec = p.out + (size_t)(tp * p.chunks + chunk) * F * plane + (size_t)yM * p.colsM +
+                 (size_t)nx * M;
+#pragma unroll
+    for (int px = 0; px < M; ++px) {
+      rec[px] = accK[px];
+      rec[plane + px] = accS[px];
+      if (MODE == kModeFull) {
+        rec[2 * plane + px] = accQ[px];
+        rec[3 * plane + px] = accP[px];
+        rec[4 * plane + px] = accL[px];
+      }
+    }
+  }
+}
+
+template <int M, int J, int MODE>
+cudaError_t launch_fused(const FusedParams& p, const CUtensorMap& tmap, cudaStream_t stream) {
+  constexpr int TY = TileRows<M>::TY;
+  using G = Geo<M, J, TY>;
+  auto kern = esrrf_fused_kernel<M, J, TY, MODE>;
+  static int attr_done = -1;  // device the attribute was last set for
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (attr_done != dev) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)G::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr_done = dev;
+  }
+  const int tiles_y = (p.H + TY - 1) / TY;
+  dim3 grid((unsigned)(p.tiles_x * tiles_y), (unsigned)(p.n_tp * p.chunks));
+  kern<<<grid, G::NT, G::SMEM_BYTES, stream>>>(tmap, p);
+  return cudaGetLastError();
+}
+
+// geometry the host needs to build the tensor map for a given (M, J)
+struct FusedGeometry {
+  int TY, IX, IY, BW, BH;
+};
+
+template <int M, int J>
+FusedGeometry fused_geometry() {
+  constexpr int TY = TileRows<M>::TY;
+  using G = Geo<M, J, TY>;
+  return FusedGeometry{TY, G::IX, G::IY, G::BW, G::BH};
+}
+
+}  // namespace nx

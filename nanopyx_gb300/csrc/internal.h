@@ -1,0 +1,79 @@
+// Internal host-side launch interfaces shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "esrrf_fused.cuh"
+
+namespace nx {
+
+// ---------------------------------------------------------------------------
+// fused eSRRF instantiations: one table entry per (M, J)
+// ---------------------------------------------------------------------------
+using FusedLaunchFn = cudaError_t (*)(const FusedParams&, const CUtensorMap&, cudaStream_t);
+struct FusedEntry {
+  FusedLaunchFn launch[3];  // indexed by FusedMode
+  FusedGeometry geo;
+};
+const FusedEntry* fused_entry(int M, int J);  // nullptr if not instantiated
+const FusedEntry* fused_entry_m1(int J);
+const FusedEntry* fused_entry_m2(int J);
+const FusedEntry* fused_entry_m3(int J);
+const FusedEntry* fused_entry_m4(int J);
+const FusedEntry* fused_entry_m5(int J);
+const FusedEntry* fused_entry_m6(int J);
+const FusedEntry* fused_entry_m8(int J);
+
+// ---------------------------------------------------------------------------
+// standalone op launchers (ops.cu)
+// ---------------------------------------------------------------------------
+cudaError_t launch_cr_shift_magnify(const float* in, int T, int H, int W, const float* shift_r,
+                                    const float* shift_c, float mag_r, float mag_c, int rowsM,
+                                    int colsM, float* out, cudaStream_t s);
+cudaError_t launch_roberts_cross(const float* in, int T, int H, int W, float* gc, float* gr,
+                                 cudaStream_t s);
+
+struct RgcScalars {
+  float tSS, tSO;
+  int start, end;  // window [start, end) on the half-pixel grid
+  int margin;
+  int sens_mode, sens_int;
+  float sens;
+};
+RgcScalars rgc_scalars(int M, float radius, float sensitivity, int pad_edges);
+
+cudaError_t launch_rgc(const float* gc, const float* gr, const float* img, int T, int rowsM,
+                       int colsM, int M, const RgcScalars& sc, int iw, float* out,
+                       cudaStream_t s);
+cudaError_t launch_gradient_radiality(const float* in, int T, int h, int w, float* gx, float* gy,
+                                      cudaStream_t s);
+struct RingCoords {
+  float x[12], y[12];
+  float radius;
+};
+RingCoords ring_coords(int M, float ring_radius);
+cudaError_t launch_radiality(const float* gx, const float* gy, const float* img_interp, int T,
+                             int h, int w, int M, const RingCoords& rc, int border, int positivity,
+                             int iw, float* out, cudaStream_t s);
+
+// temporal records: fields K, S, Q, P, L (planes of n_pixels)
+cudaError_t launch_record_push_frame(const float* frame, long long n, float* rec, int it,
+                                     cudaStream_t s);
+cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n_acc, int n_blk,
+                                cudaStream_t s);
+// combine `nchunks` consecutive records (each F planes) of one timepoint with frame
+// counts derived from nf, and write the correlations of corr_mask to out[ci*out_stride]
+cudaError_t launch_finalize(const float* rec, int F, int nchunks, int nf, long long n,
+                            int corr_mask, float* out, long long out_stride, cudaStream_t s);
+cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int corr, float* out,
+                                  cudaStream_t s);
+cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int order, float* out,
+                                 cudaStream_t s);
+// macro-pixel correction of S images in place; map scratch holds S*M*M floats
+cudaError_t launch_mpc(float* img, int S, int rowsM, int colsM, int M, float* map,
+                       cudaStream_t s);
+
+}  // namespace nx

@@ -1,0 +1,603 @@
+// Standalone Liquid-Engine ops of the eSRRF / SRRF path, temporal
+// correlations and macro-pixel correction (sm_103a).
+//
+// These follow the reference's float32 arithmetic per output pixel (they are
+// the drop-ins for the individual ops and the general fallback of the fused
+// kernel); the fused frame-loop kernel in esrrf_fused.cuh is the hot path.
+#include <cmath>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace nx {
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline unsigned grid_for(long long n, int block = kBlock) {
+  long long g = (n + block - 1) / block;
+  if (g > 1048576) g = 1048576;  // grid-stride beyond this
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+// _c_interpolate (src/include/_c_interpolation_catmull_rom.c:21-52) in float:
+// pixel-centre taps, out-of-image taps skipped, 0 outside the image.
+__device__ __forceinline__ float cr_interp(const float* __restrict__ img, float r, float c,
+                                           int rows, int cols) {
+  if (r < 0.f || r >= (float)rows || c < 0.f || c >= (float)cols) return 0.f;
+  const int r_int = (int)floorf(r - 0.5f);
+  const int c_int = (int)floorf(c - 0.5f);
+  float q = 0.f;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int cn = c_int - 1 + j;
+    if (cn < 0 || cn >= cols) continue;
+    float p = 0.f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int rn = r_int - 1 + i;
+      if (rn < 0 || rn >= rows) continue;
+      p = fmaf(__ldg(img + (size_t)rn * cols + cn), cr_cubic(r - ((float)rn + 0.5f)), p);
+    }
+    q = fmaf(p, cr_cubic(c - ((float)cn + 0.5f)), q);
+  }
+  return q;
+}
+
+__global__ void cr_shift_magnify_kernel(const float* __restrict__ in, int T, int H, int W,
+                                        const float* __restrict__ shift_r,
+                                        const float* __restrict__ shift_c, float mag_r,
+                                        float mag_c, int rowsM, int colsM,
+                                        float* __restrict__ out) {
+  const long long plane = (long long)rowsM * colsM;
+  const long long n = plane * T;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / plane);
+    const long long rem = idx - (long long)t * plane;
+    const int i = (int)(rem / colsM);
+    const int j = (int)(rem - (long long)i * colsM);
+    const float row = __fsub_rn(__fdiv_rn((float)i, mag_r), shift_r[t]);
+    const float col = __fsub_rn(__fdiv_rn((float)j, mag_c), shift_c[t]);
+    out[idx] = cr_interp(in + (size_t)t * H * W, row, col, H, W);
+  }
+}
+
+// _c_gradient_roberts_cross (src/include/_c_gradients.c:53-73), same
+// evaluation order, so bit-identical to the reference.
+__global__ void roberts_cross_kernel(const float* __restrict__ in, int T, int H, int W,
+                                     float* __restrict__ gc, float* __restrict__ gr) {
+  const long long plane = (long long)H * W;
+  const long long n = plane * T;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / plane);
+    const long long rem = idx - (long long)t * plane;
+    const int r1 = (int)(rem / W);
+    const int c1 = (int)(rem - (long long)r1 * W);
+    const int r0 = r1 > 0 ? r1 - 1 : 0;
+    const int c0 = c1 > 0 ? c1 - 1 : 0;
+    const float* f = in + (size_t)t * plane;
+    const float a = f[(size_t)r0 * W + c1];
+    const float b = f[(size_t)r1 * W + c0];
+    const float d = f[(size_t)r0 * W + c0];
+    const float e = f[(size_t)r1 * W + c1];
+    gc[idx] = __fsub_rn(__fadd_rn(__fsub_rn(a, b), e), d);
+    gr[idx] = __fsub_rn(__fadd_rn(__fadd_rn(-a, b), e), d);
+  }
+}
+
+__device__ __forceinline__ float apply_sensitivity(float r, int mode, int n, float s) {
+  if (mode == 1) {
+    const float base = r;
+    for (int k = 1; k < n; ++k) r *= base;
+  } else if (mode == 2) {
+    r = powf(r, s);
+  }
+  return r;
+}
+
+// _c_calculate_rgc (src/include/_c_sr_radial_gradient_convergence.c:17-90) per
+// output pixel, float32 as the reference (the FP64 distance weight is
+// evaluated in float), reading the given 2m-magnified gradient images.
+__global__ void rgc_kernel(const float* __restrict__ gc, const float* __restrict__ gr,
+                           const float* __restrict__ img, int T, int rowsM, int colsM, int M,
+                           RgcScalars sc, int iw, float* __restrict__ out) {
+  const long long plane = (long long)rowsM * colsM;
+  const long long n = plane * T;
+  const int grad_w = (int)((float)colsM * 2.0f);
+  const long long gplane = (long long)(2 * rowsM) * grad_w;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / plane);
+    const long long rem = idx - (long long)t * plane;
+    const int yM = (int)(rem / colsM);
+    const int xM = (int)(rem - (long long)yM * colsM);
+    if (yM < sc.margin || yM >= rowsM - sc.margin || xM < sc.margin ||
+        xM >= colsM - sc.margin) {
+      out[idx] = 0.f;
+      continue;
+    }
+    const float* Gx = gc + (size_t)t * gplane;
+    const float* Gy = gr + (size_t)t * gplane;
+    const float xc = __fdiv_rn((float)xM + 0.5f, (float)M);
+    const float yc = __fdiv_rn((float)yM + 0.5f, (float)M);
+    float rgc = 0.f, wsum = 0.f;
+    const int by = (int)(2.0f * yc), bx = (int)(2.0f * xc);
+    for (int j = sc.start; j < sc.end; ++j) {
+      const float vy = (float)(by + j) / 2.0f;
+      if (!(0.f < vy && vy <= (float)(rowsM - 1))) continue;
+      for (int i = sc.start; i < sc.end; ++i) {
+        const float vx = (float)(bx + i) / 2.0f;
+        if (!(0.f < vx && vx <= (float)(colsM - 1))) continue;
+        const float dx = vx - xc;
+        const float dy = vy - yc;
+        const float d = sqrtf(dx * dx + dy * dy);
+        if (d != 0.f && d <= sc.tSO) {
+          float pos_y = vy * (float)M * 2.0f;
+          float pos_x = vx * (float)M * 2.0f;
+          if (pos_y >= (float)rowsM * 2.0f) pos_y = (float)rowsM * 2.0f - 1.f;
+          if (pos_x >= (float)colsM * 2.0f) pos_x = (float)colsM * 2.0f - 1.f;
+          if (pos_y < 0.f) pos_y = 0.f;
+          if (pos_x < 0.f) pos_x = 0.f;
+          const size_t g = (size_t)(int)pos_y * grad_w + (int)pos_x;
+          const float gx = __ldg(Gx + g), gy = __ldg(Gy + g);
+          const float tt = d * expf(-(d * d) / sc.tSS);
+          const float w = (tt * tt) * (tt * tt);
+          wsum += w;
+          if (gx * dx + gy * dy < 0.f) {
+            float dk = fabsf(gy * dx - gx * dy) / sqrtf(gx * gx + gy * gy);
+            if (isnan(dk)) dk = d;
+            dk = 1.f - dk / d;
+            rgc += dk * w;
+          }
+        }
+      }
+    }
+    rgc = wsum > 0.f ? rgc / wsum : 0.f;
+    rgc = rgc < 0.f ? 0.f : apply_sensitivity(rgc, sc.sens_mode, sc.sens_int, sc.sens);
+    out[idx] = iw ? rgc * img[idx] : rgc;
+  }
+}
+
+// _c_gradient_radiality (src/include/_c_gradients.c:3-25)
+__global__ void gradient_radiality_kernel(const float* __restrict__ in, int T, int h, int w,
+                                          float* __restrict__ gx, float* __restrict__ gy) {
+  const long long plane = (long long)h * w;
+  const long long n = plane * T;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / plane);
+    const long long rem = idx - (long long)t * plane;
+    const int j = (int)(rem / w);
+    const int i = (int)(rem - (long long)j * w);
+    float vx = 0.f, vy = 0.f;
+    if (j >= 1 && j < h - 1 && i >= 1 && i < w - 1) {
+      const float* f = in + (size_t)t * plane;
+      vx = __fadd_rn(-f[(size_t)j * w + i - 1], f[(size_t)j * w + i + 1]);
+      vy = __fadd_rn(-f[(size_t)(j - 1) * w + i], f[(size_t)(j + 1) * w + i]);
+    }
+    gx[idx] = vx;
+    gy[idx] = vy;
+  }
+}
+
+// _c_calculate_radiality_per_subpixel (src/include/_c_sr_radiality.c:15-51)
+__global__ void radiality_kernel(const float* __restrict__ gx, const float* __restrict__ gy,
+                                 const float* __restrict__ img_interp, int T, int h, int w,
+                                 int M, RingCoords rc, int border, int positivity, int iw,
+                                 float* __restrict__ out) {
+  const int rowsM = h * M, colsM = w * M;
+  const long long plane = (long long)rowsM * colsM;
+  const long long n = plane * T;
+  const int lo_j = (1 + border) * M, hi_j = (h - 1 - border) * M;
+  const int lo_i = (1 + border) * M, hi_i = (w - 1 - border) * M;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / plane);
+    const long long rem = idx - (long long)t * plane;
+    const int j = (int)(rem / colsM);
+    const int i = (int)(rem - (long long)j * colsM);
+    if (j < lo_j || j >= hi_j || i < lo_i || i >= hi_i) {
+      out[idx] = 0.f;
+      continue;
+    }
+    const float* GX = gx + (size_t)t * h * w;
+    const float* GY = gy + (size_t)t * h * w;
+    const float xc = (float)i + 0.5f;
+    const float yc = (float)j + 0.5f;
+    float div = 0.f;
+#pragma unroll 2
+    for (int s = 0; s < 12; ++s) {
+      const float xr = rc.x[s], yr = rc.y[s];
+      const float x0 = __fadd_rn(xc, xr);
+      const float y0 = __fadd_rn(yc, yr);
+      const float ry = __fdiv_rn(y0, (float)M);
+      const float rx = __fdiv_rn(x0, (float)M);
+      const float vgx = cr_interp(GX, ry, rx, h, w);
+      const float vgy = cr_interp(GY, ry, rx, h, w);
+      const float gmag = sqrtf(vgx * vgx + vgy * vgy);
+      float dk = 0.f;
+      if (gmag != 0.f) {
+        dk = 1.f - (fabsf(vgy * (xc - x0) - vgx * (yc - y0)) / gmag) / rc.radius;
+        dk = dk * dk;
+      }
+      if (vgx * xr + vgy * yr > 0.f) div -= dk;
+      else div += dk;
+    }
+    div /= 12.f;
+    const float cgh = positivity ? fmaxf(div, 0.f) : div;
+    out[idx] = iw ? cgh * img_interp[idx] : cgh;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// temporal records  (K = first value, S = sum y, Q = sum y^2, P = sum y_t y_{t+1},
+// L = last y; y = x - K)
+// ---------------------------------------------------------------------------
+__global__ void record_push_frame_kernel(const float* __restrict__ frame, long long n,
+                                         float* __restrict__ rec, int it) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float v = frame[i];
+    if (it == 0) {
+      rec[i] = v;
+      rec[n + i] = 0.f;
+      rec[2 * n + i] = 0.f;
+      rec[3 * n + i] = 0.f;
+      rec[4 * n + i] = 0.f;
+    } else {
+      const float y = v - rec[i];
+      rec[n + i] += y;
+      rec[2 * n + i] = fmaf(y, y, rec[2 * n + i]);
+      rec[3 * n + i] = fmaf(rec[4 * n + i], y, rec[3 * n + i]);
+      rec[4 * n + i] = y;
+    }
+  }
+}
+
+struct Rec {
+  float K, S, Q, P, L;
+};
+
+// A <- A (+) B where B's frames follow A's (associative merge of shifted sums)
+__device__ __forceinline__ void rec_merge(Rec& a, const Rec& b, int na, int nb, bool full) {
+  if (nb == 0) return;
+  if (na == 0) {
+    a = b;
+    return;
+  }
+  const float d = b.K - a.K;
+  const float fnb = (float)nb;
+  if (full) {
+    a.Q = a.Q + b.Q + 2.f * d * b.S + fnb * d * d;
+    a.P = a.P + b.P + d * (2.f * b.S - b.L) + (fnb - 1.f) * d * d + a.L * d;
+    a.L = b.L + d;
+  }
+  a.S = a.S + b.S + fnb * d;
+}
+
+__global__ void record_merge_kernel(float* __restrict__ acc, const float* __restrict__ blk,
+                                    long long n, int na, int nb) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    Rec a{acc[i], acc[n + i], acc[2 * n + i], acc[3 * n + i], acc[4 * n + i]};
+    const Rec b{blk[i], blk[n + i], blk[2 * n + i], blk[3 * n + i], blk[4 * n + i]};
+    rec_merge(a, b, na, nb, true);
+    acc[i] = a.K;
+    acc[n + i] = a.S;
+    acc[2 * n + i] = a.Q;
+    acc[3 * n + i] = a.P;
+    acc[4 * n + i] = a.L;
+  }
+}
+
+__global__ void finalize_kernel(const float* __restrict__ rec, int F, int nchunks, int nf,
+                                long long n, int corr_mask, float* __restrict__ out,
+                                long long out_stride) {
+  const bool full = F >= 5;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    Rec a{0.f, 0.f, 0.f, 0.f, 0.f};
+    int na = 0;
+    for (int c = 0; c < nchunks; ++c) {
+      const int nc = (int)((long long)(c + 1) * nf / nchunks - (long long)c * nf / nchunks);
+      const float* r = rec + (size_t)c * F * n;
+      Rec b{r[i], r[n + i], 0.f, 0.f, 0.f};
+      if (full) {
+        b.Q = r[2 * n + i];
+        b.P = r[3 * n + i];
+        b.L = r[4 * n + i];
+      }
+      rec_merge(a, b, na, nc, full);
+      na += nc;
+    }
+    const float fn = (float)na;
+    const float ybar = a.S / fn;
+    int ci = 0;
+    if (corr_mask & NX_CORR_AVG) out[(ci++) * out_stride + i] = a.K + ybar;
+    if (corr_mask & NX_CORR_VAR) {
+      const float v = (a.Q - a.S * ybar) / fn;
+      out[(ci++) * out_stride + i] = v > 0.f ? v : 0.f;
+    }
+    if (corr_mask & NX_CORR_TAC2) {
+      const float num = a.P - ybar * (2.f * a.S - a.L) + (fn - 1.f) * ybar * ybar;
+      out[(ci++) * out_stride + i] = num / (fn - 1.f);
+    }
+  }
+}
+
+// sr_temporal_correlations.py:46-75,205-221 on a resident stack, float32 and
+// in numpy's order (sequential over frames, no contraction)
+__global__ void temporal_stack_kernel(const float* __restrict__ x, int T, long long n, int corr,
+                                      float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int t = 0; t < T; ++t) s = __fadd_rn(s, x[(size_t)t * n + i]);
+    const float mean = __fdiv_rn(s, (float)T);
+    if (corr == NX_CORR_AVG) {
+      out[i] = mean;
+    } else if (corr == NX_CORR_VAR) {
+      float q = 0.f;
+      for (int t = 0; t < T; ++t) {
+        const float c = __fsub_rn(x[(size_t)t * n + i], mean);
+        q = __fadd_rn(q, __fmul_rn(c, c));
+      }
+      out[i] = __fdiv_rn(q, (float)T);
+    } else {
+      float q = 0.f;
+      float prev = T > 0 ? __fsub_rn(x[i], mean) : 0.f;
+      for (int t = 1; t < T; ++t) {
+        const float c = __fsub_rn(x[(size_t)t * n + i], mean);
+        q = __fadd_rn(q, __fmul_rn(prev, c));
+        prev = c;
+      }
+      out[i] = __fdiv_rn(q, (float)(T - 1));
+    }
+  }
+}
+
+// sr_temporal_correlations.py:4-43 (orders 0, 1, -1) and :111-157 (ACRF
+// orders 2, 3, 4 without lag-time integration), float32 per pixel
+__global__ void srrf_temporal_kernel(const float* __restrict__ x, int T, long long n, int order,
+                                     float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (order == 0) {
+      float m = -INFINITY;
+      for (int t = 0; t < T; ++t) m = fmaxf(m, x[(size_t)t * n + i]);
+      out[i] = m;
+      continue;
+    }
+    if (order == -1) {
+      // sum_{t0 <= t1} r+_t0 r+_t1 / (T (T + 1) / 2), r+ = max(r, 0)
+      float s1 = 0.f, s2 = 0.f;
+      for (int t = 0; t < T; ++t) {
+        const float r = fmaxf(x[(size_t)t * n + i], 0.f);
+        s1 += r;
+        s2 = fmaf(r, r, s2);
+      }
+      const float cnt = 0.5f * (float)T * (float)(T + 1);
+      out[i] = 0.5f * (s1 * s1 + s2) / fmaxf(cnt, 1.f);
+      continue;
+    }
+    float s = 0.f;
+    for (int t = 0; t < T; ++t) s = __fadd_rn(s, x[(size_t)t * n + i]);
+    const float mean = __fdiv_rn(s, (float)T);
+    if (order == 1) {
+      out[i] = mean;
+      continue;
+    }
+    float ab = 0.f, abc = 0.f, abcd = 0.f, cd = 0.f, ac = 0.f, bd = 0.f, ad = 0.f, bc = 0.f;
+    for (int t = 0; t < T - order; ++t) {
+      const float a = __fsub_rn(x[(size_t)t * n + i], mean);
+      const float b = __fsub_rn(x[(size_t)(t + 1) * n + i], mean);
+      ab = __fadd_rn(ab, __fmul_rn(a, b));
+      if (order == 3) {
+        const float c = __fsub_rn(x[(size_t)(t + 2) * n + i], mean);
+        abc = __fadd_rn(__fadd_rn(abc, __fmul_rn(a, b)), c);
+      }
+      if (order == 4) {
+        const float c = __fsub_rn(x[(size_t)(t + 2) * n + i], mean);
+        const float d = __fsub_rn(x[(size_t)(t + 3) * n + i], mean);
+        abcd = __fadd_rn(abcd, __fmul_rn(__fmul_rn(__fmul_rn(a, b), c), d));
+        cd = __fadd_rn(cd, __fmul_rn(c, d));
+        ac = __fadd_rn(ac, __fmul_rn(a, c));
+        bd = __fadd_rn(bd, __fmul_rn(b, d));
+        ad = __fadd_rn(ad, __fmul_rn(a, d));
+        bc = __fadd_rn(bc, __fmul_rn(b, c));
+      }
+    }
+    float v;
+    if (order == 3) v = fabsf(abc);
+    else if (order == 4) v = fabsf(abcd - ab * cd - ac * bd - ad * bc);
+    else v = fabsf(ab);
+    out[i] = __fdiv_rn(v, (float)T);
+  }
+}
+
+// macro-pixel map: block (s, py); thread t sums phase px = t % M over its
+// columns and all macro-pixel rows (Kahan); fixed-order block reduction
+__global__ void mpc_map_kernel(const float* __restrict__ img, int rowsM, int colsM, int M,
+                               float* __restrict__ map) {
+  extern __shared__ float red[];
+  const int s = blockIdx.x;
+  const int py = blockIdx.y;
+  const int rows = rowsM / M, cols = colsM / M;
+  const float* f = img + (size_t)s * rowsM * colsM;
+  float sum = 0.f, comp = 0.f;
+  for (int ry = 0; ry < rows; ++ry) {
+    const float* row = f + (size_t)(ry * M + py) * colsM;
+    for (int x = threadIdx.x; x < cols * M; x += blockDim.x) {
+      const float yk = row[x] - comp;
+      const float tk = sum + yk;
+      comp = (tk - sum) - yk;
+      sum = tk;
+    }
+  }
+  red[threadIdx.x] = sum;
+  __syncthreads();
+  if ((int)threadIdx.x < M) {
+    float tot = 0.f, c2 = 0.f;
+    for (int t = threadIdx.x; t < (int)blockDim.x; t += M) {
+      const float yk = red[t] - c2;
+      const float tk = tot + yk;
+      c2 = (tk - tot) - yk;
+      tot = tk;
+    }
+    map[(size_t)s * M * M + py * M + threadIdx.x] = tot / (float)(rows * cols);
+  }
+}
+
+__global__ void mpc_apply_kernel(float* __restrict__ img, int S, int rowsM, int colsM, int M,
+                                 const float* __restrict__ map) {
+  const long long plane = (long long)rowsM * colsM;
+  const long long n = plane * S;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(idx / plane);
+    const long long rem = idx - (long long)s * plane;
+    const int yM = (int)(rem / colsM);
+    const int xM = (int)(rem - (long long)yM * colsM);
+    const float c = map[(size_t)s * M * M + (yM % M) * M + (xM % M)];
+    if (c != 0.f) img[idx] = __fdiv_rn(img[idx], c);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+cudaError_t launch_cr_shift_magnify(const float* in, int T, int H, int W, const float* shift_r,
+                                    const float* shift_c, float mag_r, float mag_c, int rowsM,
+                                    int colsM, float* out, cudaStream_t s) {
+  const long long n = (long long)T * rowsM * colsM;
+  if (n == 0) return cudaSuccess;
+  cr_shift_magnify_kernel<<<grid_for(n), kBlock, 0, s>>>(in, T, H, W, shift_r, shift_c, mag_r,
+                                                         mag_c, rowsM, colsM, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roberts_cross(const float* in, int T, int H, int W, float* gc, float* gr,
+                                 cudaStream_t s) {
+  const long long n = (long long)T * H * W;
+  if (n == 0) return cudaSuccess;
+  roberts_cross_kernel<<<grid_for(n), kBlock, 0, s>>>(in, T, H, W, gc, gr);
+  return cudaGetLastError();
+}
+
+RgcScalars rgc_scalars(int M, float radius, float sensitivity, int pad_edges) {
+  RgcScalars sc{};
+  const float sigma = (float)((double)radius / 2.355);
+  const float fwhm = radius;
+  sc.tSS = 2.0f * sigma * sigma;
+  sc.tSO = 2.0f * sigma + 1.0f;
+  sc.start = -(int)(2.0f * fwhm);
+  sc.end = (int)(2.0f * fwhm + 1.0f);
+  sc.margin = pad_edges ? 0 : (int)((double)fwhm * (double)M);
+  sc.sens = sensitivity;
+  if (!(sensitivity > 1.0f)) {
+    sc.sens_mode = 0;
+  } else if (sensitivity == std::floor(sensitivity) && sensitivity <= 16.0f) {
+    sc.sens_mode = 1;
+    sc.sens_int = (int)sensitivity;
+  } else {
+    sc.sens_mode = 2;
+  }
+  return sc;
+}
+
+cudaError_t launch_rgc(const float* gc, const float* gr, const float* img, int T, int rowsM,
+                       int colsM, int M, const RgcScalars& sc, int iw, float* out,
+                       cudaStream_t s) {
+  const long long n = (long long)T * rowsM * colsM;
+  if (n == 0) return cudaSuccess;
+  rgc_kernel<<<grid_for(n), kBlock, 0, s>>>(gc, gr, img, T, rowsM, colsM, M, sc, iw, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gradient_radiality(const float* in, int T, int h, int w, float* gx, float* gy,
+                                      cudaStream_t s) {
+  const long long n = (long long)T * h * w;
+  if (n == 0) return cudaSuccess;
+  gradient_radiality_kernel<<<grid_for(n), kBlock, 0, s>>>(in, T, h, w, gx, gy);
+  return cudaGetLastError();
+}
+
+RingCoords ring_coords(int M, float ring_radius) {
+  // _le_radiality.pyx:92-104: float32 ring of 12 points at ringRadius * m
+  RingCoords rc{};
+  rc.radius = (float)((double)ring_radius * (double)M);
+  const float step = (float)((3.14159265358979323846 * 2.0) / 12.0);
+  for (int k = 0; k < 12; ++k) {
+    const float arg = step * (float)k;
+    rc.x[k] = (float)(std::cos((double)arg) * (double)rc.radius);
+    rc.y[k] = (float)(std::sin((double)arg) * (double)rc.radius);
+  }
+  return rc;
+}
+
+cudaError_t launch_radiality(const float* gx, const float* gy, const float* img_interp, int T,
+                             int h, int w, int M, const RingCoords& rc, int border, int positivity,
+                             int iw, float* out, cudaStream_t s) {
+  const long long n = (long long)T * h * M * w * M;
+  if (n == 0) return cudaSuccess;
+  radiality_kernel<<<grid_for(n), kBlock, 0, s>>>(gx, gy, img_interp, T, h, w, M, rc, border,
+                                                  positivity, iw, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_record_push_frame(const float* frame, long long n, float* rec, int it,
+                                     cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  record_push_frame_kernel<<<grid_for(n), kBlock, 0, s>>>(frame, n, rec, it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n_acc, int n_blk,
+                                cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  record_merge_kernel<<<grid_for(n), kBlock, 0, s>>>(acc, blk, n, n_acc, n_blk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const float* rec, int F, int nchunks, int nf, long long n,
+                            int corr_mask, float* out, long long out_stride, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  finalize_kernel<<<grid_for(n), kBlock, 0, s>>>(rec, F, nchunks, nf, n, corr_mask, out,
+                                                 out_stride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int corr, float* out,
+                                  cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  temporal_stack_kernel<<<grid_for(n), kBlock, 0, s>>>(stack, T, n, corr, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int order, float* out,
+                                 cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  srrf_temporal_kernel<<<grid_for(n), kBlock, 0, s>>>(stack, T, n, order, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mpc(float* img, int S, int rowsM, int colsM, int M, float* map,
+                       cudaStream_t s) {
+  if ((long long)S * rowsM * colsM == 0) return cudaSuccess;
+  const int block = M <= 32 ? 32 * M : ((1024 / M) * M);
+  mpc_map_kernel<<<dim3((unsigned)S, (unsigned)M), block, block * sizeof(float), s>>>(
+      img, rowsM, colsM, M, map);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const long long n = (long long)S * rowsM * colsM;
+  mpc_apply_kernel<<<grid_for(n), kBlock, 0, s>>>(img, S, rowsM, colsM, M, map);
+  return cudaGetLastError();
+}
+
+}  // namespace nx

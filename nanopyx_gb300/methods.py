@@ -1,0 +1,246 @@
+"""User-level methods: ``eSRRF``, ``SRRF``, ``Workflow`` and the parameter sweep.
+
+Drop-ins for (paths inside the reference project):
+
+* ``eSRRF`` -- ``src/nanopyx/methods/esrrf/eSRRF_workflow.py:12-121``
+* ``SRRF`` -- ``src/nanopyx/methods/srrf/SRRF_workflow.py:9-76``
+* ``Workflow`` -- ``src/nanopyx/methods/workflow.py:4-139``
+* ``esrrf_parameter_sweep`` -- the reconstruction grid of
+  ``src/nanopyx/core/analysis/parameter_sweep.py:17-97`` (one eSRRF run per
+  (sensitivity, radius) pair).  Its QnR scoring (ErrorMap, FRC, decorrelation)
+  is not part of this engine.
+
+``eSRRF`` runs the whole timepoint loop on the device: one fused kernel per
+call produces every timepoint's temporal correlation(s), then the macro-pixel
+correction runs on the device too; only the final images come back.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._device import get_plan, stream_ptr, to_device_stack, workspace
+from .transform import (GradientRobertsCross, Radiality, ShiftAndMagnify,  # noqa: F401
+                        macro_pixel_corrector)
+
+__all__ = ["eSRRF", "SRRF", "Workflow", "ESRRFAccumulator", "esrrf_parameter_sweep", "run_esrrf_parameter_sweep",
+           "esrrf_device"]
+
+
+def _corr_list(temporal_correlation):
+    names = [temporal_correlation] if isinstance(temporal_correlation, str) else list(
+        temporal_correlation)
+    if not names or any(n not in N.CORR_BITS for n in names):
+        raise ValueError("Type of correlation must be AVG, VAR or TAC2")
+    return names
+
+
+def esrrf_device(stack: torch.Tensor, magnification: int = 5, radius: float = 1.5,
+                 sensitivity: float = 1, frames_per_timepoint: int = 0,
+                 temporal_correlation="AVG", doIntensityWeighting: bool = True,
+                 macro_pixel_correction: bool = True, check_status: bool = True):
+    """eSRRF on a resident (T, H, W) float32 CUDA tensor.
+
+    Returns a (n_corr, n_timepoints, H*m, W*m) CUDA tensor, correlations in the
+    order requested.  Asynchronous on the current stream unless ``check_status``.
+    """
+    names = _corr_list(temporal_correlation)
+    mask = 0
+    for n in names:
+        mask |= N.CORR_BITS[n]
+    T, H, W = stack.shape
+    if T < 1:
+        raise ValueError("eSRRF needs at least one frame")
+    fpt = T if frames_per_timepoint == 0 or frames_per_timepoint > T else int(frames_per_timepoint)
+    if fpt < 0:
+        raise ValueError("frames_per_timepoint must be >= 0")
+    n_tp = T // fpt + (1 if T % fpt else 0)
+    m = int(magnification)
+    plan = get_plan(H, W, m, radius, sensitivity, doIntensityWeighting)
+    L = N.lib()
+    ws = workspace(L.nx_esrrf_workspace_bytes(plan.handle, T, fpt, mask), stack.device)
+    order = [b for b in ("AVG", "VAR", "TAC2") if mask & N.CORR_BITS[b]]
+    out = torch.empty((len(order), n_tp, H * m, W * m), dtype=torch.float32, device=stack.device)
+    N.check(L.nx_esrrf_run(plan.handle, stack.data_ptr(), T, fpt, mask,
+                           1 if macro_pixel_correction else 0, out.data_ptr(), ws.data_ptr(),
+                           ws.numel(), stream_ptr()), "eSRRF")
+    if check_status:
+        N.check(L.nx_workspace_status(ws.data_ptr(), stream_ptr()), "eSRRF")
+    idx = [order.index(n) for n in names]
+    if idx != list(range(len(order))):
+        out = out[idx]
+    return out
+
+
+def eSRRF(image, magnification: int = 5, radius: float = 1.5, sensitivity: float = 1,
+          frames_per_timepoint: int = 0, temporal_correlation="AVG", use_fht: bool = False,
+          doIntensityWeighting: bool = True, macro_pixel_correction: bool = True,
+          pad_edges: bool = False, _force_run_type=None):
+    """eSRRF reconstruction (reference signature and semantics).
+
+    ``temporal_correlation`` may also be a sequence of names; the result is then
+    a tuple with one squeezed array per name, computed in a single pass.
+    ``pad_edges`` has no effect on this (non-FHT) path, as in the reference.
+    """
+    if use_fht:
+        raise NotImplementedError("use_fht=True (Fourier interpolation) is not implemented")
+    names = _corr_list(temporal_correlation)
+    st = to_device_stack(image)
+    out = esrrf_device(st.t, magnification, radius, sensitivity, frames_per_timepoint, names,
+                       doIntensityWeighting, macro_pixel_correction)
+    res = st.out(out)
+    if st.from_numpy:
+        parts = [np.squeeze(res[i].astype(np.float32)) for i in range(len(names))]
+    else:
+        parts = [torch.squeeze(res[i]) for i in range(len(names))]
+    return parts[0] if isinstance(temporal_correlation, str) else tuple(parts)
+
+
+def SRRF(image, magnification: int = 5, ringRadius: float = 0.5, border: int = 0,
+         radialityPositivityConstraint: bool = True, doIntensityWeighting: bool = True,
+         macro_pixel_correction: bool = True, _force_run_type=None):
+    """SRRF per-frame radiality stack (T, H*m, W*m), macro-pixel corrected per frame."""
+    st = to_device_stack(image)
+    mag = ShiftAndMagnify().run(st.t, 0, 0, magnification, magnification)
+    rad = Radiality().run(st.t, mag, magnification=magnification, ringRadius=ringRadius,
+                          border=border, radialityPositivityConstraint=radialityPositivityConstraint,
+                          doIntensityWeighting=doIntensityWeighting)
+    if macro_pixel_correction:
+        rad = macro_pixel_corrector(rad, magnification)
+    return st.out(rad)
+
+
+class Workflow:
+    """Sequential op chain with ``PREV_RETURN_VALUE_<i>_<j>`` argument wiring."""
+
+    def __init__(self, *args):
+        self._methods = []
+        self._return_values = []
+        for arg in args:
+            if isinstance(arg, tuple) and len(arg) == 3:
+                self._methods.append((arg[0], arg[1], arg[2]))
+            else:
+                raise TypeError("Each arg must be a tuple of 3 items (fn, args, kwargs)")
+
+    @staticmethod
+    def _resolve(v, values):
+        if isinstance(v, str) and "PREV_RETURN_VALUE" in v:
+            idx = [int(i) for i in v.split("_") if i.isdigit()]
+            return values[idx[0]][idx[1]]
+        return v
+
+    def run(self, _force_run_type=None):
+        fn = None
+        for fn, args, kwargs in self._methods:
+            sane_args = [self._resolve(a, self._return_values) for a in args]
+            kw = {k: self._resolve(v, self._return_values) for k, v in kwargs.items()}
+            kw["run_type"] = _force_run_type
+            rv = fn.run(*sane_args, **kw)
+            self._return_values.append(rv if isinstance(rv, tuple) else (rv,))
+        return self._return_values[-1], fn._last_runtype, fn._last_time
+
+    def calculate(self, _force_run_type=None):
+        output, _, _ = self.run(_force_run_type=_force_run_type)
+        return output
+
+
+def esrrf_parameter_sweep(img, magnification: int = 2, sensitivities=(1, 2), radii=(1, 1.5),
+                          temporal_correlation: str = "AVG", frames_per_timepoint: int = 0,
+                          doIntensityWeighting: bool = True, macro_pixel_correction: bool = False):
+    """Reconstruction grid of the eSRRF parameter sweep.
+
+    Returns an array (len(sensitivities), len(radii), n_timepoints, H*m, W*m)
+    (squeezed over timepoints like ``eSRRF``).  The input is uploaded once and
+    each (sensitivity, radius) pair runs as one fused pass; the reference runs
+    a full, independent eSRRF_ST per pair (parameter_sweep.py:35-37).
+    For the single-launch batched form see ``nanopyx_gb300.engine``.
+    """
+    st = to_device_stack(img)
+    outs = []
+    for s in sensitivities:
+        row = []
+        for r in radii:
+            o = esrrf_device(st.t, magnification, r, s, frames_per_timepoint,
+                             [temporal_correlation], doIntensityWeighting,
+                             macro_pixel_correction)[0]
+            row.append(o)
+        outs.append(torch.stack(row))
+    res = torch.stack(outs)
+    res = st.out(res)
+    if st.from_numpy and res.shape[2] == 1:
+        res = res[:, :, 0]
+    return res
+
+
+def run_esrrf_parameter_sweep(*args, **kwargs):
+    raise NotImplementedError(
+        "QnR scoring (ErrorMap / FRC / decorrelation) of the parameter sweep is outside this "
+        "engine; esrrf_parameter_sweep() returns the reconstruction grid it scores")
+
+
+class ESRRFAccumulator:
+    """Device-resident temporal state of one eSRRF reconstruction.
+
+    Frame blocks are pushed as they arrive (``push``); the per-pixel shifted
+    sums (K, S, Q, P, L) stay on the device between pushes, so a reconstruction
+    over many blocks never holds its per-frame stack anywhere.  ``finalize``
+    returns the requested correlations (each (H*m, W*m)), macro-pixel corrected
+    if asked, with the same arithmetic as ``eSRRF`` over one timepoint.
+    """
+
+    def __init__(self, H: int, W: int, magnification: int = 5, radius: float = 1.5,
+                 sensitivity: float = 1, doIntensityWeighting: bool = True, device=None):
+        from ._device import require_cuda
+
+        self.device = device if device is not None else require_cuda()
+        self.H, self.W, self.m = int(H), int(W), int(magnification)
+        self.plan = get_plan(H, W, magnification, radius, sensitivity, doIntensityWeighting)
+        L = N.lib()
+        self.state = torch.empty(L.nx_esrrf_accum_bytes(self.plan.handle), dtype=torch.uint8,
+                                 device=self.device)
+        self.frames = 0
+        self._ws = None
+
+    def _workspace(self, nbytes):
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = workspace(nbytes, self.device)
+        return self._ws
+
+    def push(self, block) -> None:
+        """Add a (T_block, H, W) block (NumPy or CUDA tensor) to the state."""
+        st = to_device_stack(block)
+        T, H, W = st.shape
+        if (H, W) != (self.H, self.W):
+            raise ValueError("block frame size does not match the accumulator")
+        L = N.lib()
+        ws = self._workspace(L.nx_esrrf_push_workspace_bytes(self.plan.handle, T))
+        N.check(L.nx_esrrf_accum_push(self.plan.handle, st.ptr(), T, self.frames,
+                                      self.state.data_ptr(), ws.data_ptr(), ws.numel(),
+                                      stream_ptr()), "eSRRF push")
+        self._keep = st.t  # the input must outlive the asynchronous push
+        self.frames += T
+
+    def finalize_device(self, temporal_correlation="AVG", macro_pixel_correction: bool = True):
+        names = _corr_list(temporal_correlation)
+        mask = 0
+        for n in names:
+            mask |= N.CORR_BITS[n]
+        if self.frames < 1:
+            raise ValueError("no frames were pushed")
+        order = [b for b in ("AVG", "VAR", "TAC2") if mask & N.CORR_BITS[b]]
+        out = torch.empty((len(order), self.H * self.m, self.W * self.m), dtype=torch.float32,
+                          device=self.device)
+        L = N.lib()
+        ws = self._workspace(256 + 4 * 3 * self.m * self.m + 256)
+        N.check(L.nx_esrrf_accum_finalize(self.plan.handle, self.state.data_ptr(), self.frames,
+                                          mask, 1 if macro_pixel_correction else 0,
+                                          out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                          stream_ptr()), "eSRRF finalize")
+        return out[[order.index(n) for n in names]]
+
+    def finalize(self, temporal_correlation="AVG", macro_pixel_correction: bool = True):
+        out = self.finalize_device(temporal_correlation, macro_pixel_correction)
+        N.check(N.lib().nx_workspace_status(self._ws.data_ptr(), stream_ptr()), "eSRRF")
+        res = out.cpu().numpy()
+        return res[0] if isinstance(temporal_correlation, str) else tuple(res)

@@ -1,0 +1,283 @@
+"""The Liquid-Engine ops of the eSRRF / SRRF path, on the GB300 CUDA path.
+
+Drop-ins for (paths inside the reference project):
+
+* ``ShiftAndMagnify`` (exported as ``CRShiftAndMagnify``)
+  -- ``src/nanopyx/core/transform/_le_interpolation_catmull_rom.pyx:17``
+* ``GradientRobertsCross`` -- ``.../_le_roberts_cross_gradients.pyx:16``
+* ``RadialGradientConvergence`` -- ``.../_le_radial_gradient_convergence.pyx:16``
+* ``Radiality`` -- ``.../_le_radiality.pyx:27``
+* ``eSRRF_ST`` -- ``.../_le_esrrf.pyx:21`` (class ``eSRRF``)
+* ``calculate_eSRRF_temporal_correlations`` /
+  ``calculate_SRRF_temporal_correlations``
+  -- ``src/nanopyx/core/transform/sr_temporal_correlations.py:4-75``
+* ``macro_pixel_corrector`` -- ``src/nanopyx/core/transform/mpcorrector.pyx:7``
+
+Ownership follows the reference: inputs are never modified; NumPy in gives
+NumPy out; a CUDA tensor in gives a CUDA tensor out (computed on the current
+stream).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._device import (DeviceStack, check_image, get_plan, require_cuda, stream_ptr,
+                      to_device_stack, workspace)
+from .liquid import LiquidEngine
+
+__all__ = ["ShiftAndMagnify", "CRShiftAndMagnify", "GradientRobertsCross",
+           "RadialGradientConvergence", "Radiality", "eSRRF_ST", "value2array",
+           "calculate_eSRRF_temporal_correlations", "calculate_SRRF_temporal_correlations",
+           "macro_pixel_corrector", "check_image"]
+
+
+def value2array(v, n_frames: int) -> np.ndarray:
+    """Reference ``value2array`` (``__interpolation_tools__.py:30-40``)."""
+    if type(v) in (int, float) or np.isscalar(v):
+        v = np.ones(n_frames, dtype=np.float32) * np.float32(v)
+    return np.asarray(v, dtype=np.float32)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+def _empty(shape, like: DeviceStack) -> torch.Tensor:
+    return torch.empty(shape, dtype=torch.float32, device=like.t.device)
+
+
+class ShiftAndMagnify(LiquidEngine):
+    """Catmull-Rom shift and magnify (``row = i / mag - shift``, pixel-centre taps)."""
+
+    _designation = "ShiftMagnify_catmull_rom"
+
+    def run(self, image, shift_row, shift_col, magnification_row, magnification_col,
+            run_type=None):
+        return self._run(image, shift_row, shift_col, magnification_row, magnification_col,
+                         run_type=run_type)
+
+    def benchmark(self, image, shift_row, shift_col, magnification_row, magnification_col):
+        return super().benchmark(image, shift_row, shift_col, magnification_row,
+                                 magnification_col)
+
+    def _run_cuda(self, image, shift_row, shift_col, magnification_row, magnification_col):
+        img = to_device_stack(image)
+        T, H, W = img.shape
+        mr = np.float32(magnification_row)
+        mc = np.float32(magnification_col)
+        rowsM = int(np.float32(H) * mr)
+        colsM = int(np.float32(W) * mc)
+        sr = torch.from_numpy(value2array(shift_row, T).copy()).to(img.t.device)
+        sc = torch.from_numpy(value2array(shift_col, T).copy()).to(img.t.device)
+        if sr.numel() != T or sc.numel() != T:
+            raise ValueError("shift arrays must have one value per frame")
+        out = _empty((T, rowsM, colsM), img)
+        N.check(N.lib().nx_cr_shift_magnify(img.ptr(), T, H, W, _ptr(sr), _ptr(sc), float(mr),
+                                            float(mc), _ptr(out), stream_ptr()),
+                "ShiftAndMagnify")
+        return img.out(out)
+
+
+CRShiftAndMagnify = ShiftAndMagnify
+
+
+class GradientRobertsCross(LiquidEngine):
+    """Roberts-Cross gradients with top/left clamp; returns (gradient_col, gradient_row)."""
+
+    _designation = "GradientRobertsCross"
+
+    def run(self, image, run_type=None):
+        return self._run(image, run_type=run_type)
+
+    def benchmark(self, image):
+        return super().benchmark(image)
+
+    def _run_cuda(self, image):
+        img = to_device_stack(image)
+        T, H, W = img.shape
+        gc = _empty((T, H, W), img)
+        gr = _empty((T, H, W), img)
+        N.check(N.lib().nx_roberts_cross(img.ptr(), T, H, W, _ptr(gc), _ptr(gr), stream_ptr()),
+                "GradientRobertsCross")
+        return img.out(gc), img.out(gr)
+
+
+class RadialGradientConvergence(LiquidEngine):
+    """RGC on 2m-magnified gradients and the m-magnified image."""
+
+    _designation = "RadialGradientConvergence"
+
+    def run(self, gradient_col_interp, gradient_row_interp, image_interp, magnification: int = 5,
+            radius: float = 1.5, sensitivity: float = 1, doIntensityWeighting: bool = True,
+            pad_edges: bool = False, run_type=None):
+        return self._run(gradient_col_interp, gradient_row_interp, image_interp, magnification,
+                         radius, sensitivity, doIntensityWeighting, pad_edges=pad_edges,
+                         run_type=run_type)
+
+    def benchmark(self, gradient_col_interp, gradient_row_interp, image_interp,
+                  magnification: int = 5, radius: float = 1.5, sensitivity: float = 1,
+                  doIntensityWeighting: bool = True, pad_edges: bool = False):
+        return super().benchmark(gradient_col_interp, gradient_row_interp, image_interp,
+                                 magnification, radius, sensitivity, doIntensityWeighting,
+                                 pad_edges=pad_edges)
+
+    def _run_cuda(self, gci, gri, image_interp, magnification=5, radius=1.5, sensitivity=1,
+                  doIntensityWeighting=True, pad_edges=False):
+        gc = to_device_stack(gci)
+        gr = to_device_stack(gri)
+        im = to_device_stack(image_interp)
+        T, rowsM, colsM = im.shape
+        if gc.shape != (T, 2 * rowsM, 2 * colsM) or gr.shape != gc.shape:
+            raise ValueError("gradient images must be (T, 2*rowsM, 2*colsM) of the magnified image")
+        out = _empty((T, rowsM, colsM), im)
+        N.check(N.lib().nx_rgc(gc.ptr(), gr.ptr(), im.ptr(), T, rowsM, colsM, int(magnification),
+                               float(np.float32(radius)), float(np.float32(sensitivity)),
+                               1 if doIntensityWeighting else 0, 1 if pad_edges else 0,
+                               _ptr(out), stream_ptr()),
+                "RadialGradientConvergence")
+        return im.out(out)
+
+
+class Radiality(LiquidEngine):
+    """SRRF radiality over a 12-point ring of radius ringRadius * magnification."""
+
+    _designation = "Radiality"
+
+    def run(self, image, image_interp, magnification: int = 5, ringRadius: float = 0.5,
+            border: int = 0, radialityPositivityConstraint: bool = True,
+            doIntensityWeighting: bool = True, run_type=None):
+        return self._run(image, image_interp, magnification, ringRadius, border,
+                         radialityPositivityConstraint, doIntensityWeighting, run_type=run_type)
+
+    def benchmark(self, image, image_interp, magnification: int = 5, ringRadius: float = 0.5,
+                  border: int = 0, radialityPositivityConstraint: bool = True,
+                  doIntensityWeighting: bool = True):
+        return super().benchmark(image, image_interp, magnification, ringRadius, border,
+                                 radialityPositivityConstraint, doIntensityWeighting)
+
+    def _run_cuda(self, image, image_interp, magnification=5, ringRadius=0.5, border=0,
+                  radialityPositivityConstraint=True, doIntensityWeighting=True):
+        img = to_device_stack(image)
+        imi = to_device_stack(image_interp)
+        T, h, w = img.shape
+        m = int(magnification)
+        if imi.shape != (T, h * m, w * m):
+            raise ValueError("image_interp must be (T, h*m, w*m)")
+        out = _empty((T, h * m, w * m), img)
+        nb = N.lib().nx_radiality_workspace_bytes(T, h, w)
+        ws = workspace(nb, img.t.device)
+        N.check(N.lib().nx_radiality(img.ptr(), imi.ptr(), T, h, w, m, float(ringRadius),
+                                     int(border), 1 if radialityPositivityConstraint else 0,
+                                     1 if doIntensityWeighting else 0, _ptr(out), _ptr(ws),
+                                     ws.numel(), stream_ptr()),
+                "Radiality")
+        return img.out(out)
+
+
+class eSRRF_ST(LiquidEngine):
+    """eSRRF single task: per-frame RGC maps (T, H*m, W*m) from one fused kernel.
+
+    ``pad_edges`` is accepted and, as on the reference's non-FHT path
+    (``_le_esrrf.pyx:194`` does not forward it), has no effect.
+    """
+
+    _designation = "eSRRF_ST"
+
+    def run(self, image, magnification: int = 5, radius: float = 1.5, sensitivity: float = 1,
+            use_fht: bool = False, doIntensityWeighting: bool = True, pad_edges: bool = False,
+            run_type=None):
+        return self._run(image, magnification=magnification, radius=radius,
+                         sensitivity=sensitivity, use_fht=use_fht,
+                         doIntensityWeighting=doIntensityWeighting, pad_edges=pad_edges,
+                         run_type=run_type)
+
+    def benchmark(self, image, magnification: int = 5, radius: float = 1.5,
+                  sensitivity: float = 1, use_fht: bool = False,
+                  doIntensityWeighting: bool = True, pad_edges: bool = False):
+        return super().benchmark(image, magnification=magnification, radius=radius,
+                                 sensitivity=sensitivity, use_fht=use_fht,
+                                 doIntensityWeighting=doIntensityWeighting, pad_edges=pad_edges)
+
+    def _run_cuda(self, image, magnification=5, radius=1.5, sensitivity=1, use_fht=False,
+                  doIntensityWeighting=True, pad_edges=False):
+        if use_fht:
+            raise NotImplementedError("use_fht=True (Fourier interpolation) is not implemented")
+        img = to_device_stack(image)
+        T, H, W = img.shape
+        m = int(magnification)
+        plan = get_plan(H, W, m, radius, sensitivity, doIntensityWeighting)
+        out = _empty((T, H * m, W * m), img)
+        L = N.lib()
+        ws = workspace(L.nx_esrrf_st_workspace_bytes(plan.handle, T), img.t.device)
+        N.check(L.nx_esrrf_st(plan.handle, img.ptr(), T, _ptr(out), _ptr(ws), ws.numel(),
+                              stream_ptr()), "eSRRF_ST")
+        N.check(L.nx_workspace_status(_ptr(ws), stream_ptr()), "eSRRF_ST")
+        return img.out(out)
+
+
+# ---------------------------------------------------------------------------
+# temporal correlations
+# ---------------------------------------------------------------------------
+def _stack3(im) -> DeviceStack:
+    if isinstance(im, torch.Tensor):
+        t = im.to(torch.float32)
+        if t.ndim != 3:
+            raise AssertionError("input must be a 3-D (T, H, W) stack")
+        return DeviceStack(t.contiguous().to(require_cuda()) if not t.is_cuda else t.contiguous(),
+                           not t.is_cuda)
+    a = np.array(im, dtype="float32")
+    if a.ndim != 3:
+        raise AssertionError("input must be a 3-D (T, H, W) stack")
+    return DeviceStack(torch.from_numpy(np.ascontiguousarray(a)).to(require_cuda()), True)
+
+
+def calculate_eSRRF_temporal_correlations(im, correlation: str):
+    """AVG / VAR / TAC2 over axis 0 (numpy float32 order)."""
+    if correlation not in N.CORR_BITS:
+        raise ValueError("Type of correlation must be AVG, VAR or TAC2")
+    st = _stack3(im)
+    T = st.shape[0]
+    out = torch.empty(st.shape[1:], dtype=torch.float32, device=st.t.device)
+    N.check(N.lib().nx_temporal_correlation(st.ptr(), T, out.numel(), N.CORR_BITS[correlation],
+                                            _ptr(out), stream_ptr()),
+            "temporal correlation")
+    return st.out(out)
+
+
+def calculate_SRRF_temporal_correlations(im, order: int = 1, do_integrate_lag_times: bool = 0):
+    """Orders 0 (max), 1 (mean), -1 (pairwise product sum), 2/3/4 (ACRF)."""
+    st = _stack3(im)
+    assert order <= 4
+    if do_integrate_lag_times and order not in (0, 1, -1):
+        raise NotImplementedError("ACRF with lag-time integration is not implemented")
+    if order < -1:
+        raise ValueError("order must be -1, 0, 1, 2, 3 or 4")
+    T = st.shape[0]
+    out = torch.empty(st.shape[1:], dtype=torch.float32, device=st.t.device)
+    N.check(N.lib().nx_srrf_temporal_correlation(st.ptr(), T, out.numel(), int(order), _ptr(out),
+                                                 stream_ptr()),
+            "SRRF temporal correlation")
+    return st.out(out)
+
+
+def macro_pixel_corrector(img, magnification: int):
+    """Per-slice macro-pixel correction; returns a corrected float32 copy."""
+    if isinstance(img, torch.Tensor):
+        t = img.to(torch.float32)
+        src_np = not t.is_cuda
+        t = t.to(require_cuda()).contiguous().clone()
+    else:
+        a = np.asarray(img).astype(np.float32)
+        src_np = True
+        t = torch.from_numpy(np.ascontiguousarray(a)).to(require_cuda())
+    if t.ndim != 3:
+        raise ValueError("Buffer has wrong number of dimensions (expected 3)")
+    S, rowsM, colsM = t.shape
+    m = int(magnification)
+    ws = workspace(N.lib().nx_macro_pixel_workspace_bytes(S, m), t.device)
+    N.check(N.lib().nx_macro_pixel_correct(_ptr(t), S, rowsM, colsM, m, _ptr(ws), ws.numel(),
+                                           stream_ptr()),
+            "macro_pixel_corrector")
+    return t.cpu().numpy() if src_np else t

@@ -1,0 +1,402 @@
+"""FP64 NumPy restatement of the reference's eSRRF / SRRF CPU path.
+
+TEST INFRASTRUCTURE ONLY: the oracle.  Only ``tests/``, ``__graft_entry__.smoke``
+and ``bench.py``'s CPU-baseline legs import it, as the checker; the product
+package ``nanopyx_gb300`` never does.
+
+Every function restates, in float64 arithmetic, one reference routine (paths
+inside the reference project):
+
+* ``cubic`` / ``cr_resample`` / ``cr_points``  -- Catmull-Rom (Keys, a = 0.5)
+  ``src/include/_c_interpolation_catmull_rom.c:6-18`` (``_c_cubic``) and
+  ``:21-52`` (``_c_interpolate``): pixel-centre convention, taps outside the
+  image are skipped (not renormalised), 0 outside ``[0, rows) x [0, cols)``;
+  sampling grid of ``ShiftAndMagnify`` (``row = i / mag - shift``,
+  ``src/nanopyx/core/transform/_le_interpolation_catmull_rom.pyx:143-160``).
+* ``roberts_cross``  -- ``src/include/_c_gradients.c:53-73``.
+* ``rgc_params`` / ``radial_gradient_convergence``  --
+  ``src/nanopyx/core/transform/_le_radial_gradient_convergence.pyx:85-115``
+  and ``src/include/_c_sr_radial_gradient_convergence.c:4-90``.
+* ``esrrf_st``  -- ``src/nanopyx/core/transform/_le_esrrf.pyx:172-196``.
+* ``temporal_correlation``  --
+  ``src/nanopyx/core/transform/sr_temporal_correlations.py:46-75,205-221``.
+* ``macro_pixel_correct``  -- ``src/nanopyx/core/transform/mpcorrector.pyx:26-73``.
+* ``esrrf``  -- ``src/nanopyx/methods/esrrf/eSRRF_workflow.py:58-121``.
+* ``gradient_radiality`` / ``radiality`` / ``srrf``  --
+  ``src/include/_c_gradients.c:3-25``, ``src/include/_c_sr_radiality.c:6-51``,
+  ``src/nanopyx/core/transform/_le_radiality.pyx:86-125`` and
+  ``src/nanopyx/methods/srrf/SRRF_workflow.py:50-76``.
+
+Scalar parameters are taken exactly as the reference forms them (its float32
+``sigma``, ``tSS``, ``tSO``, ring coordinates); the arithmetic on pixel data
+is float64 throughout, so this is the "exact" answer the float32 reference and
+the GPU path are both measured against.
+
+The RGC reads the 2m-magnified gradient images only at rows / columns that are
+multiples of ``m`` (plus the clamped last row / column), so ``esrrf_st``
+evaluates the gradient interpolation at exactly those positions instead of
+materialising the full ``(2Hm, 2Wm)`` images; the values are the same ones the
+reference reads.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+F32 = np.float32
+
+
+# ----------------------------------------------------------------------------
+# Catmull-Rom
+# ----------------------------------------------------------------------------
+def cubic(v):
+    v = np.abs(np.asarray(v, dtype=np.float64))
+    a = 0.5
+    z = np.zeros_like(v)
+    m1 = v < 1
+    m2 = (v >= 1) & (v < 2)
+    z[m1] = v[m1] * v[m1] * (v[m1] * (-a + 2) + (a - 3)) + 1
+    vv = v[m2]
+    z[m2] = -a * vv * vv * vv + 5 * a * vv * vv - 8 * a * vv + 4 * a
+    return z
+
+
+def _cr_weight_matrix(coords, n):
+    """(len(coords), n) tap-weight matrix of _c_interpolate along one axis."""
+    coords = np.asarray(coords, dtype=np.float64)
+    Wm = np.zeros((coords.size, n), dtype=np.float64)
+    inside = (coords >= 0) & (coords < n)
+    base = np.floor(coords - 0.5).astype(np.int64)
+    for t in range(4):
+        nb = base - 1 + t
+        ok = inside & (nb >= 0) & (nb < n)
+        idx = np.nonzero(ok)[0]
+        Wm[idx, nb[idx]] += cubic(coords[idx] - (nb[idx] + 0.5))
+    return Wm, inside
+
+
+def cr_resample(img2d, row_coords, col_coords):
+    """Separable CR evaluation of one frame on a (rows x cols) coordinate grid."""
+    img = np.asarray(img2d, dtype=np.float64)
+    Wr, _ = _cr_weight_matrix(row_coords, img.shape[0])
+    Wc, _ = _cr_weight_matrix(col_coords, img.shape[1])
+    return Wr @ img @ Wc.T
+
+
+def cr_shift_magnify(stack, shift_row, shift_col, mag_row, mag_col):
+    """ShiftAndMagnify (reference sampling grid) for a (T, H, W) stack."""
+    stack = np.asarray(stack)
+    T, H, W = stack.shape
+    rowsM = int(H * F32(mag_row))
+    colsM = int(W * F32(mag_col))
+    rr = np.arange(rowsM, dtype=np.float64) / float(F32(mag_row)) - float(F32(shift_row))
+    cc = np.arange(colsM, dtype=np.float64) / float(F32(mag_col)) - float(F32(shift_col))
+    out = np.empty((T, rowsM, colsM), dtype=np.float64)
+    for t in range(T):
+        out[t] = cr_resample(stack[t], rr, cc)
+    return out
+
+
+def cr_points(img2d, r, c):
+    """Pointwise CR evaluation at coordinate arrays r, c (same shape)."""
+    img = np.asarray(img2d, dtype=np.float64)
+    rows, cols = img.shape
+    r = np.asarray(r, dtype=np.float64)
+    c = np.asarray(c, dtype=np.float64)
+    inside = (r >= 0) & (r < rows) & (c >= 0) & (c < cols)
+    r_int = np.floor(r - 0.5).astype(np.int64)
+    c_int = np.floor(c - 0.5).astype(np.int64)
+    q = np.zeros(r.shape, dtype=np.float64)
+    for j in range(4):
+        cn = c_int - 1 + j
+        okc = (cn >= 0) & (cn < cols)
+        wc = cubic(c - (cn + 0.5))
+        p = np.zeros(r.shape, dtype=np.float64)
+        for i in range(4):
+            rn = r_int - 1 + i
+            ok = okc & (rn >= 0) & (rn < rows)
+            vals = np.where(ok, img[np.clip(rn, 0, rows - 1), np.clip(cn, 0, cols - 1)], 0.0)
+            p += vals * cubic(r - (rn + 0.5))
+        q += np.where(okc, p * wc, 0.0)
+    return np.where(inside, q, 0.0)
+
+
+# ----------------------------------------------------------------------------
+# gradients
+# ----------------------------------------------------------------------------
+def roberts_cross(stack):
+    """Roberts-Cross with top/left clamp; returns (gradient_col, gradient_row)."""
+    a = np.asarray(stack, dtype=np.float64)
+    if a.ndim == 2:
+        a = a[None]
+    up = np.concatenate([a[:, :1], a[:, :-1]], axis=1)          # [r0, c1]
+    left = np.concatenate([a[:, :, :1], a[:, :, :-1]], axis=2)  # [r1, c0]
+    upleft = np.concatenate([up[:, :, :1], up[:, :, :-1]], axis=2)  # [r0, c0]
+    gc = up - left + a - upleft
+    gr = -up + left + a - upleft
+    return gc, gr
+
+
+def gradient_radiality(frame):
+    """Central differences on rows/cols 1..n-2, zero elsewhere (_c_gradients.c:3-25)."""
+    f = np.asarray(frame, dtype=np.float64)
+    gx = np.zeros_like(f)
+    gy = np.zeros_like(f)
+    gx[1:-1, 1:-1] = -f[1:-1, :-2] + f[1:-1, 2:]
+    gy[1:-1, 1:-1] = -f[:-2, 1:-1] + f[2:, 1:-1]
+    return gx, gy
+
+
+# ----------------------------------------------------------------------------
+# RGC
+# ----------------------------------------------------------------------------
+def rgc_params(radius):
+    """Scalars exactly as _le_radial_gradient_convergence.pyx:85-92 forms them."""
+    sigma = F32(float(radius) / 2.355)
+    fwhm = F32(radius)
+    tSS = F32(F32(2) * sigma * sigma)
+    tSO = F32(F32(2) * sigma + F32(1))
+    start = -int(F32(2.0) * fwhm)
+    end = int(F32(2.0) * fwhm + F32(1))
+    return dict(sigma=sigma, fwhm=fwhm, tSS=tSS, tSO=tSO, start=start, end=end)
+
+
+def rgc_margin(radius, magnification, pad_edges=False):
+    return 0 if pad_edges else int(float(F32(radius)) * magnification)
+
+
+def _rgc_frame(gx_at, gy_at, rowsM, colsM, m, p, margin):
+    """One frame of RGC (before intensity weighting).
+
+    ``gx_at(py_idx, px_idx)`` returns gradient values at integer positions of the
+    2m-magnified grid (arrays broadcast against each other).
+    """
+    yM = np.arange(margin, rowsM - margin)
+    xM = np.arange(margin, colsM - margin)
+    out = np.zeros((rowsM, colsM), dtype=np.float64)
+    if yM.size == 0 or xM.size == 0:
+        return out
+    yc = ((yM + 0.5) / m)[:, None]
+    xc = ((xM + 0.5) / m)[None, :]
+    tSS = float(p["tSS"])
+    tSO = float(p["tSO"])
+    rgc = np.zeros((yM.size, xM.size))
+    wsum = np.zeros((yM.size, xM.size))
+    by = np.trunc(2.0 * yc).astype(np.int64)
+    bx = np.trunc(2.0 * xc).astype(np.int64)
+    for j in range(p["start"], p["end"]):
+        vy = (by + j) / 2.0
+        oky = (vy > 0) & (vy <= rowsM - 1)
+        posy = np.clip(vy * m * 2, 0, rowsM * 2 - 1).astype(np.int64)
+        for i in range(p["start"], p["end"]):
+            vx = (bx + i) / 2.0
+            okx = (vx > 0) & (vx <= colsM - 1)
+            dx = vx - xc
+            dy = vy - yc
+            d = np.sqrt(dx * dx + dy * dy)
+            ok = oky & okx & (d != 0) & (d <= tSO)
+            if not ok.any():
+                continue
+            posx = np.clip(vx * m * 2, 0, colsM * 2 - 1).astype(np.int64)
+            Gx = gx_at(posy, posx)
+            Gy = gy_at(posy, posx)
+            dsafe = np.where(d == 0, 1.0, d)
+            w = (dsafe * np.exp(-(dsafe * dsafe) / tSS)) ** 4
+            w = np.where(ok, w, 0.0)
+            wsum += w
+            gdotr = Gx * dx + Gy * dy
+            gn = np.sqrt(Gx * Gx + Gy * Gy)
+            with np.errstate(invalid="ignore", divide="ignore"):
+                dk = np.abs(Gy * dx - Gx * dy) / gn
+            dk = np.where(np.isnan(dk), dsafe, dk)
+            dk = 1.0 - dk / dsafe
+            rgc += np.where(ok & (gdotr < 0), dk * w, 0.0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rgc = np.where(wsum > 0, rgc / np.where(wsum > 0, wsum, 1.0), 0.0)
+    s = float(F32(p["sensitivity"]))
+    rgc = np.where(rgc < 0, 0.0, rgc)
+    if s > 1:
+        rgc = rgc ** s
+    out[margin:rowsM - margin, margin:colsM - margin] = rgc
+    return out
+
+
+def radial_gradient_convergence(gc_interp, gr_interp, image_interp, magnification=5,
+                                radius=1.5, sensitivity=1, doIntensityWeighting=True,
+                                pad_edges=False):
+    """Standalone RGC op on given 2m-magnified gradients and m-magnified image."""
+    gc_interp = np.asarray(gc_interp, dtype=np.float64)
+    gr_interp = np.asarray(gr_interp, dtype=np.float64)
+    image_interp = np.asarray(image_interp, dtype=np.float64)
+    if gc_interp.ndim == 2:
+        gc_interp, gr_interp = gc_interp[None], gr_interp[None]
+    if image_interp.ndim == 2:
+        image_interp = image_interp[None]
+    T, rowsM, colsM = image_interp.shape
+    p = rgc_params(radius)
+    p["sensitivity"] = sensitivity
+    margin = rgc_margin(radius, magnification, pad_edges)
+    gw = int(colsM * 2)
+    out = np.zeros((T, rowsM, colsM))
+    for t in range(T):
+        gcf = gc_interp[t].reshape(-1)
+        grf = gr_interp[t].reshape(-1)
+        f = _rgc_frame(lambda y, x: gcf[y * gw + x], lambda y, x: grf[y * gw + x],
+                       rowsM, colsM, magnification, p, margin)
+        out[t] = f * image_interp[t] if doIntensityWeighting else f
+    return out
+
+
+def esrrf_st(stack, magnification=5, radius=1.5, sensitivity=1, doIntensityWeighting=True):
+    """eSRRF single task: (T, H, W) -> per-frame RGC maps (T, H*m, W*m)."""
+    stack = np.asarray(stack)
+    if stack.ndim == 2:
+        stack = stack[None]
+    T, H, W = stack.shape
+    m = int(magnification)
+    rowsM, colsM = H * m, W * m
+    p = rgc_params(radius)
+    p["sensitivity"] = sensitivity
+    margin = rgc_margin(radius, m)
+    # magnified intensity
+    rr = np.arange(rowsM) / float(m)
+    cc = np.arange(colsM) / float(m)
+    # gradient interpolation only where RGC reads: rows/cols k*m (k >= 0),
+    # clamped to 2*m*H - 1 by the RGC kernel
+    ky = np.unique(np.clip(np.arange(0, 2 * H + 2) * m, 0, 2 * rowsM - 1))
+    kx = np.unique(np.clip(np.arange(0, 2 * W + 2) * m, 0, 2 * colsM - 1))
+    ry = ky / (2.0 * m)
+    rx = kx / (2.0 * m)
+    lut_y = np.full(2 * rowsM, -1, dtype=np.int64)
+    lut_y[ky] = np.arange(ky.size)
+    lut_x = np.full(2 * colsM, -1, dtype=np.int64)
+    lut_x[kx] = np.arange(kx.size)
+    gcs, grs = roberts_cross(stack)
+    out = np.zeros((T, rowsM, colsM))
+    for t in range(T):
+        mag = cr_resample(stack[t], rr, cc)
+        gxi = cr_resample(gcs[t], ry, rx)
+        gyi = cr_resample(grs[t], ry, rx)
+        f = _rgc_frame(lambda y, x: gxi[lut_y[y], lut_x[x]],
+                       lambda y, x: gyi[lut_y[y], lut_x[x]],
+                       rowsM, colsM, m, p, margin)
+        out[t] = f * mag if doIntensityWeighting else f
+    return out
+
+
+# ----------------------------------------------------------------------------
+# temporal correlations and macro-pixel correction
+# ----------------------------------------------------------------------------
+def temporal_correlation(stack, correlation):
+    x = np.asarray(stack, dtype=np.float64)
+    if correlation == "AVG":
+        return x.mean(axis=0)
+    if correlation == "VAR":
+        return x.var(axis=0)
+    if correlation == "TAC2":
+        c = x - x.mean(axis=0)
+        return (c[:-1] * c[1:]).mean(axis=0)
+    raise ValueError("Type of correlation must be AVG, VAR or TAC2")
+
+
+def macro_pixel_correct(img, magnification):
+    a = np.array(img, dtype=np.float64)
+    if a.ndim == 2:
+        a = a[None]
+    S, rowsM, colsM = a.shape
+    m = int(magnification)
+    rows, cols = rowsM // m, colsM // m
+    for s in range(S):
+        blk = a[s, :rows * m, :cols * m].reshape(rows, m, cols, m)
+        cmap = blk.sum(axis=(0, 2)) / (rows * cols)
+        corr = np.tile(cmap, (rowsM // m + 1, colsM // m + 1))[:rowsM, :colsM]
+        nz = corr != 0
+        a[s][nz] /= corr[nz]
+    return a
+
+
+def esrrf(stack, magnification=5, radius=1.5, sensitivity=1, frames_per_timepoint=0,
+          temporal_correlation_name="AVG", doIntensityWeighting=True,
+          macro_pixel_correction=True):
+    stack = np.asarray(stack)
+    if stack.ndim == 2:
+        stack = stack[None]
+    T = stack.shape[0]
+    fpt = T if frames_per_timepoint == 0 or frames_per_timepoint > T else frames_per_timepoint
+    ntp = T // fpt + (1 if T % fpt else 0)
+    outs = []
+    for i in range(ntp):
+        rgc = esrrf_st(stack[fpt * i: fpt * (i + 1)], magnification, radius, sensitivity,
+                       doIntensityWeighting)
+        tc = temporal_correlation(rgc, temporal_correlation_name)
+        if macro_pixel_correction:
+            tc = macro_pixel_correct(tc, magnification)[0]
+        outs.append(tc)
+    return np.squeeze(np.stack(outs))
+
+
+# ----------------------------------------------------------------------------
+# SRRF radiality
+# ----------------------------------------------------------------------------
+def ring_coordinates(magnification, ring_radius, n=12):
+    """Float32 ring offsets exactly as _le_radiality.pyx:92-104 forms them."""
+    rr = F32(float(ring_radius) * magnification)
+    step = F32((np.pi * 2.0) / n)
+    xs = np.array([F32(np.cos(float(F32(step * F32(k)))) * float(rr)) for k in range(n)], dtype=np.float32)
+    ys = np.array([F32(np.sin(float(F32(step * F32(k)))) * float(rr)) for k in range(n)], dtype=np.float32)
+    return xs, ys, rr
+
+
+def radiality(stack, image_interp, magnification=5, ringRadius=0.5, border=0,
+              radialityPositivityConstraint=True, doIntensityWeighting=True):
+    stack = np.asarray(stack)
+    if stack.ndim == 2:
+        stack = stack[None]
+    image_interp = np.asarray(image_interp, dtype=np.float64)
+    if image_interp.ndim == 2:
+        image_interp = image_interp[None]
+    T, h, w = stack.shape
+    m = int(magnification)
+    xs, ys, rr = ring_coordinates(m, ringRadius)
+    out = np.zeros((T, h * m, w * m))
+    j0, j1 = (1 + border) * m, (h - 1 - border) * m
+    i0, i1 = (1 + border) * m, (w - 1 - border) * m
+    if j1 <= j0 or i1 <= i0:
+        return out
+    jj = np.arange(j0, j1)[:, None].astype(np.float64)
+    ii = np.arange(i0, i1)[None, :].astype(np.float64)
+    yc = jj + 0.5
+    xc = ii + 0.5
+    for t in range(T):
+        gx, gy = gradient_radiality(stack[t])
+        acc = np.zeros((j1 - j0, i1 - i0))
+        for k in range(xs.size):
+            x0 = xc + float(xs[k])
+            y0 = yc + float(ys[k])
+            vgx = cr_points(gx, y0 / m + 0 * x0, x0 / m + 0 * y0)
+            vgy = cr_points(gy, y0 / m + 0 * x0, x0 / m + 0 * y0)
+            gmag = np.sqrt(vgx * vgx + vgy * vgy)
+            with np.errstate(invalid="ignore", divide="ignore"):
+                dk = 1 - (np.abs(vgy * (xc - x0) - vgx * (yc - y0)) / gmag) / float(rr)
+            dk = np.where(gmag != 0, dk * dk, 0.0)
+            sgn = (vgx * float(xs[k]) + vgy * float(ys[k])) > 0
+            acc += np.where(sgn, -dk, dk)
+        acc /= xs.size
+        if radialityPositivityConstraint:
+            acc = np.maximum(acc, 0)
+        res = np.zeros((h * m, w * m))
+        res[j0:j1, i0:i1] = acc
+        out[t] = res * image_interp[t] if doIntensityWeighting else res
+    return out
+
+
+def srrf(stack, magnification=5, ringRadius=0.5, border=0, radialityPositivityConstraint=True,
+         doIntensityWeighting=True, macro_pixel_correction=True):
+    stack = np.asarray(stack)
+    if stack.ndim == 2:
+        stack = stack[None]
+    mag = cr_shift_magnify(stack, 0, 0, magnification, magnification)
+    rad = radiality(stack, mag, magnification, ringRadius, border,
+                    radialityPositivityConstraint, doIntensityWeighting)
+    if macro_pixel_correction:
+        rad = macro_pixel_correct(rad, magnification)
+    return rad

@@ -1,0 +1,132 @@
+"""Generate the golden vectors in ``tests/golden/golden.npz``.
+
+Runs the reference's OWN compiled CPU path (``oracle/_ref``, built from the
+reference sources by ``oracle/ref_build.py``) on small seeded inputs and stores
+inputs + outputs.  The reference's test-suite has no numeric fixtures for this
+path (its eSRRF/SRRF tests are smoke tests on a network dataset), so these
+vectors are what pins both the FP64 oracle and the CUDA path.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from nanopyx_gb300.synthetic import blinking_stack  # noqa: E402
+from oracle import ref_build  # noqa: E402
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
+
+# (magnification, radius, sensitivity, intensity weighting)
+ESRRF_ST_CASES = [
+    (5, 1.5, 1, True), (5, 1.5, 2, True), (2, 1.5, 1, True), (4, 2.5, 2, True),
+    (3, 1.0, 1, False), (5, 2.0, 4, True), (1, 1.5, 1, True), (6, 1.5, 1, True),
+    (8, 1.0, 1, True), (7, 1.5, 1, True), (5, 3.5, 1, True), (2, 0.4, 1, True),
+    (4, 1.25, 1.5, True),
+]
+
+
+def main():
+    if not ref_build.available():
+        ref_build.build()
+    R = ref_build.load()
+    g = {}
+
+    # eSRRF_ST per-frame maps
+    x = blinking_stack(2, 16, 20, 5, seed=11)
+    g["esrrf_st/input"] = x
+    for k, (m, r, s, iw) in enumerate(ESRRF_ST_CASES):
+        out = R["eSRRF_ST"](verbose=False).run(x, magnification=m, radius=r, sensitivity=s,
+                                               doIntensityWeighting=iw, run_type="Threaded")
+        g[f"esrrf_st/{k}"] = np.asarray(out, dtype=np.float32)
+    g["esrrf_st/cases"] = np.array(ESRRF_ST_CASES, dtype=np.float64)
+
+    # full eSRRF(): timepoints of 5 frames (last one short), AVG/VAR/TAC2, MPC on/off
+    x = blinking_stack(12, 24, 20, 6, seed=12)
+    g["esrrf/input"] = x
+    m, r, s, fpt = 5, 1.5, 2, 5
+    for corr in ("AVG", "VAR", "TAC2"):
+        for mpc in (True, False):
+            outs = []
+            for i in range(0, x.shape[0], fpt):
+                st = R["eSRRF_ST"](verbose=False).run(x[i:i + fpt], magnification=m, radius=r,
+                                                      sensitivity=s, run_type="Threaded")
+                tc = np.asarray(R["calculate_eSRRF_temporal_correlations"](st, corr))
+                if mpc:
+                    tc = R["macro_pixel_corrector"](np.expand_dims(tc, 0), magnification=m)[0]
+                outs.append(np.asarray(tc, dtype=np.float32))
+            g[f"esrrf/{corr}/{int(mpc)}"] = np.stack(outs)
+
+    # Catmull-Rom ShiftAndMagnify
+    x = blinking_stack(2, 9, 11, 2, seed=13)
+    g["cr/input"] = x
+    cr = R["CRShiftAndMagnify"](verbose=False)
+    g["cr/0"] = cr.run(x, 0, 0, 5, 5, run_type="Threaded")
+    g["cr/1"] = cr.run(x, 0.3, -1.2, 2.5, 3.0, run_type="Threaded")
+    g["cr/2"] = cr.run(x, 0, 0, 10, 10, run_type="Threaded")
+
+    # Roberts-Cross
+    gc, gr = R["GradientRobertsCross"](verbose=False).run(x, run_type="Threaded")
+    g["robx/gc"] = np.asarray(gc)
+    g["robx/gr"] = np.asarray(gr)
+
+    # standalone RGC on the reference's own magnified gradients
+    x = blinking_stack(2, 12, 14, 3, seed=14)
+    g["rgc/input"] = x
+    m = 4
+    gc, gr = R["GradientRobertsCross"](verbose=False).run(x, run_type="Threaded")
+    gci = cr.run(gc, 0, 0, 2 * m, 2 * m, run_type="Threaded")
+    gri = cr.run(gr, 0, 0, 2 * m, 2 * m, run_type="Threaded")
+    mag = cr.run(x, 0, 0, m, m, run_type="Threaded")
+    g["rgc/gci"], g["rgc/gri"], g["rgc/mag"] = gci, gri, mag
+    rgc = R["RadialGradientConvergence"](verbose=False)
+    g["rgc/0"] = rgc.run(gci, gri, mag, magnification=m, radius=1.5, sensitivity=1,
+                         run_type="Threaded")
+    g["rgc/1"] = rgc.run(gci, gri, mag, magnification=m, radius=1.5, sensitivity=2,
+                         pad_edges=True, run_type="Threaded")
+    g["rgc/2"] = rgc.run(gci, gri, mag, magnification=m, radius=2.0, sensitivity=1,
+                         doIntensityWeighting=False, run_type="Threaded")
+
+    # SRRF radiality (+ the reference's CR-magnified intensity)
+    x = blinking_stack(2, 14, 16, 3, seed=15)
+    g["srrf/input"] = x
+    rad = R["Radiality"](verbose=False)
+    for k, (m, ring, border, pos) in enumerate([(5, 0.5, 0, True), (4, 1.0, 1, False),
+                                                 (2, 0.5, 0, True)]):
+        mag = cr.run(x, 0, 0, m, m, run_type="Threaded")
+        out = rad.run(x, mag, magnification=m, ringRadius=ring, border=border,
+                      radialityPositivityConstraint=pos, run_type="Threaded")
+        g[f"srrf/{k}"] = np.asarray(out)
+        g[f"srrf/{k}/mpc"] = np.asarray(R["macro_pixel_corrector"](np.asarray(out), magnification=m))
+
+    # temporal correlations
+    rng = np.random.default_rng(16)
+    x = (rng.random((7, 10, 12)) * 3 + 0.5).astype(np.float32)
+    g["temporal/input"] = x
+    for corr in ("AVG", "VAR", "TAC2"):
+        g[f"temporal/{corr}"] = np.asarray(R["calculate_eSRRF_temporal_correlations"](x, corr))
+    xs = (rng.random((9, 8, 10)) * 2 - 0.5).astype(np.float32)
+    g["srrf_temporal/input"] = xs
+    for order in (0, 1, -1, 2, 3, 4):
+        g[f"srrf_temporal/{order}"] = np.asarray(
+            R["calculate_SRRF_temporal_correlations"](xs, order), dtype=np.float32)
+
+    # macro-pixel correction
+    x = (rng.random((2, 20, 25)) + 0.1).astype(np.float32)
+    x[0, :, :3] = 0.0
+    g["mpc/input"] = x
+    g["mpc/5"] = np.asarray(R["macro_pixel_corrector"](x, magnification=5))
+
+    g = {k: (np.asarray(v, dtype=np.float32) if k != "esrrf_st/cases" else v) for k, v in g.items()}
+    np.savez_compressed(OUT, **g)
+    print(f"wrote {OUT}: {len(g)} arrays, {os.path.getsize(OUT) / 1e6:.2f} MB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,198 @@
+"""GPU parity of the CUDA path against the reference's golden vectors and the oracle.
+
+Bar (floating point): max |got - ref| / (max(ref) - min(ref)) <= 1e-4, the
+tolerance the eSRRF/SRRF path is held to; integer-exact steps (Roberts-Cross)
+are compared bit for bit.  Every call goes through the package, which calls the
+C ABI of libnanopyx_gb300.so.
+"""
+import numpy as np
+import pytest
+import torch
+
+import nanopyx_gb300 as nx
+from conftest import rel_err
+from nanopyx_gb300 import _native
+from nanopyx_gb300.synthetic import blinking_stack
+from oracle import esrrf_np as O
+from oracle import ref_build
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    _native.lib()
+    yield
+    torch.cuda.synchronize()
+
+
+def test_esrrf_st_matches_reference(golden):
+    x = golden["esrrf_st/input"]
+    for k, (m, r, s, iw) in enumerate(golden["esrrf_st/cases"]):
+        got = nx.eSRRF_ST(verbose=False).run(x, magnification=int(m), radius=float(r),
+                                             sensitivity=float(s), doIntensityWeighting=bool(iw))
+        assert isinstance(got, np.ndarray) and got.dtype == np.float32
+        e = rel_err(got, golden[f"esrrf_st/{k}"])
+        assert e <= TOL, (k, m, r, s, iw, e)
+
+
+@pytest.mark.parametrize("corr", ["AVG", "VAR", "TAC2"])
+@pytest.mark.parametrize("mpc", [0, 1])
+def test_esrrf_matches_reference(golden, corr, mpc):
+    x = golden["esrrf/input"]
+    got = nx.eSRRF(x, magnification=5, radius=1.5, sensitivity=2, frames_per_timepoint=5,
+                   temporal_correlation=corr, macro_pixel_correction=bool(mpc))
+    ref = golden[f"esrrf/{corr}/{mpc}"]
+    assert got.shape == ref.shape
+    assert rel_err(got, ref) <= TOL
+
+
+def test_multi_correlation_single_pass_equals_separate_calls(golden):
+    x = golden["esrrf/input"]
+    v, t, a = nx.eSRRF(x, 5, 1.5, 2, frames_per_timepoint=5,
+                       temporal_correlation=("VAR", "TAC2", "AVG"))
+    for name, arr in (("VAR", v), ("TAC2", t), ("AVG", a)):
+        one = nx.eSRRF(x, 5, 1.5, 2, frames_per_timepoint=5, temporal_correlation=name)
+        assert np.array_equal(arr, one), name
+
+
+def test_shift_magnify_matches_reference(golden):
+    x = golden["cr/input"]
+    op = nx.CRShiftAndMagnify(verbose=False)
+    assert rel_err(op.run(x, 0, 0, 5, 5), golden["cr/0"]) <= 1e-6
+    assert rel_err(op.run(x, 0.3, -1.2, 2.5, 3.0), golden["cr/1"]) <= 1e-6
+    assert rel_err(op.run(x, 0, 0, 10, 10), golden["cr/2"]) <= 1e-6
+
+
+def test_roberts_cross_bit_exact(golden):
+    gc, gr = nx.GradientRobertsCross(verbose=False).run(golden["cr/input"])
+    assert np.array_equal(gc, golden["robx/gc"])
+    assert np.array_equal(gr, golden["robx/gr"])
+
+
+def test_rgc_standalone_matches_reference(golden):
+    gci, gri, mag = golden["rgc/gci"], golden["rgc/gri"], golden["rgc/mag"]
+    op = nx.RadialGradientConvergence(verbose=False)
+    assert rel_err(op.run(gci, gri, mag, 4, 1.5, 1), golden["rgc/0"]) <= TOL
+    assert rel_err(op.run(gci, gri, mag, 4, 1.5, 2, pad_edges=True), golden["rgc/1"]) <= TOL
+    assert rel_err(op.run(gci, gri, mag, 4, 2.0, 1, doIntensityWeighting=False),
+                   golden["rgc/2"]) <= TOL
+
+
+def test_radiality_and_srrf_match_reference(golden):
+    x = golden["srrf/input"]
+    for k, (m, ring, border, pos) in enumerate([(5, 0.5, 0, True), (4, 1.0, 1, False),
+                                                 (2, 0.5, 0, True)]):
+        mag = nx.CRShiftAndMagnify(verbose=False).run(x, 0, 0, m, m)
+        got = nx.Radiality(verbose=False).run(x, mag, magnification=m, ringRadius=ring,
+                                              border=border, radialityPositivityConstraint=pos)
+        assert rel_err(got, golden[f"srrf/{k}"]) <= TOL, k
+        full = nx.SRRF(x, magnification=m, ringRadius=ring, border=border,
+                       radialityPositivityConstraint=pos)
+        assert rel_err(full, golden[f"srrf/{k}/mpc"]) <= TOL, k
+
+
+def test_temporal_correlations_match_numpy_reference(golden):
+    x = golden["temporal/input"]
+    for corr in ("AVG", "VAR", "TAC2"):
+        got = nx.calculate_eSRRF_temporal_correlations(x, corr)
+        assert rel_err(got, golden[f"temporal/{corr}"]) <= 1e-6, corr
+    with pytest.raises(ValueError):
+        nx.calculate_eSRRF_temporal_correlations(x, "ACF")
+    xs = golden["srrf_temporal/input"]
+    for order in (0, 1, -1, 2, 3, 4):
+        got = nx.calculate_SRRF_temporal_correlations(xs, order)
+        assert rel_err(got, golden[f"srrf_temporal/{order}"]) <= 1e-5, order
+
+
+def test_macro_pixel_corrector_matches_reference(golden):
+    got = nx.macro_pixel_corrector(golden["mpc/input"], 5)
+    assert rel_err(got, golden["mpc/5"]) <= 1e-6
+
+
+@pytest.mark.parametrize("T,H,W,m,r", [
+    (1, 3, 5, 2, 1.5), (2, 17, 31, 5, 1.5), (3, 2, 9, 2, 1.0), (2, 31, 17, 4, 2.0),
+    (1, 1, 7, 3, 1.5), (3, 20, 21, 5, 1.5), (2, 33, 65, 2, 2.5), (1, 9, 40, 6, 1.0),
+])
+def test_odd_sizes_against_oracle(T, H, W, m, r):
+    x = blinking_stack(T, H, W, max(1, H * W // 40), seed=H * 100 + W)
+    got = nx.eSRRF_ST(verbose=False).run(x, magnification=m, radius=r, sensitivity=1)
+    ref = O.esrrf_st(x, m, r, 1)
+    if np.ptp(ref) == 0:
+        assert np.array_equal(got, ref.astype(np.float32))
+    else:
+        assert rel_err(got, ref) <= TOL
+
+
+def test_results_are_deterministic():
+    x = blinking_stack(8, 64, 64, 20, seed=21)
+    a = nx.eSRRF(x, 5, 1.5, 2, temporal_correlation=("VAR", "TAC2"))
+    b = nx.eSRRF(x, 5, 1.5, 2, temporal_correlation=("VAR", "TAC2"))
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+
+
+def test_tensor_in_tensor_out_stays_on_device():
+    x = torch.from_numpy(blinking_stack(4, 32, 32, 8, seed=22)).cuda()
+    out = nx.eSRRF(x, 4, 1.5, 1)
+    assert isinstance(out, torch.Tensor) and out.is_cuda and tuple(out.shape) == (128, 128)
+    ref = nx.eSRRF(x.cpu().numpy(), 4, 1.5, 1)
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_streamed_blocks_equal_one_shot():
+    x = blinking_stack(23, 40, 48, 10, seed=23)
+    one = nx.eSRRF(x, 5, 1.5, 1, temporal_correlation=("AVG", "VAR", "TAC2"))
+    acc = nx.ESRRFAccumulator(40, 48, 5, 1.5, 1)
+    for a, b in ((0, 7), (7, 8), (8, 20), (20, 23)):
+        acc.push(x[a:b])
+    got = acc.finalize(("AVG", "VAR", "TAC2"))
+    for u, v in zip(got, one):
+        assert rel_err(u, v) <= 1e-5
+
+
+def test_timepoints_equal_separate_calls():
+    x = blinking_stack(30, 48, 40, 12, seed=24)
+    full = nx.eSRRF(x, 4, 2.0, 2, frames_per_timepoint=12, temporal_correlation="TAC2")
+    assert full.shape == (3, 192, 160)
+    for i, (a, b) in enumerate(((0, 12), (12, 24), (24, 30))):
+        one = nx.eSRRF(x[a:b], 4, 2.0, 2, temporal_correlation="TAC2")
+        assert rel_err(full[i], one) <= 1e-5
+
+
+def test_cfg0_against_reference():
+    """100 frames x 100 x 100, 40 emitters, m=5, R=1.5, s=1, AVG + MPC."""
+    x = blinking_stack(100, 100, 100, 40, seed=0)
+    got = nx.eSRRF(x, magnification=5, radius=1.5, sensitivity=1, temporal_correlation="AVG")
+    if ref_build.available():
+        R = ref_build.load()
+        st = R["eSRRF_ST"](verbose=False).run(x, magnification=5, radius=1.5, sensitivity=1,
+                                              run_type="Threaded")
+        tc = R["calculate_eSRRF_temporal_correlations"](st, "AVG")
+        ref = R["macro_pixel_corrector"](np.expand_dims(np.asarray(tc), 0), magnification=5)[0]
+    else:
+        ref = O.esrrf(x[:10], 5, 1.5, 1, 0, "AVG")
+        got = nx.eSRRF(x[:10], magnification=5, radius=1.5, sensitivity=1)
+    assert rel_err(got, ref) <= TOL
+
+
+def test_large_frame_properties():
+    """512 x 512 frames at m=5, s=2: VAR >= 0, margins 0, finite, block split invariant."""
+    x = blinking_stack(12, 512, 512, 400, seed=1)
+    var, tac = nx.eSRRF(x, 5, 1.5, 2, frames_per_timepoint=6,
+                        temporal_correlation=("VAR", "TAC2"), macro_pixel_correction=False)
+    assert var.shape == (2, 2560, 2560)
+    assert np.isfinite(var).all() and np.isfinite(tac).all()
+    assert (var >= 0).all()
+    mg = int(1.5 * 5)
+    assert not var[:, :mg].any() and not var[:, -mg:].any()
+    assert not var[:, :, :mg].any() and not var[:, :, -mg:].any()
+    second = nx.eSRRF(x[6:], 5, 1.5, 2, temporal_correlation="VAR", macro_pixel_correction=False)
+    assert rel_err(var[1], second) <= 1e-5
+    # the FP64 oracle on a crop of frames reproduces the per-frame maps
+    st = nx.eSRRF_ST(verbose=False).run(x[:1], 5, 1.5, 2)
+    ref = O.esrrf_st(x[:1, :96, :96], 5, 1.5, 2)
+    # interior of the crop only (the crop's own border differs from the full frame's)
+    assert rel_err(st[0, 40:400, 40:400], ref[0, 40:400, 40:400]) <= TOL

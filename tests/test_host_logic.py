@@ -1,0 +1,78 @@
+"""Host-side logic that needs no GPU: input normalisation, argument checks,
+Workflow wiring, the synthetic generator."""
+import numpy as np
+import pytest
+import torch
+
+import nanopyx_gb300 as nx
+from nanopyx_gb300 import methods, synthetic
+from nanopyx_gb300.liquid import LiquidEngine
+
+
+def test_check_image_shapes_and_dtype():
+    a = nx.check_image(np.ones((4, 5), dtype=np.uint16))
+    assert a.shape == (1, 4, 5) and a.dtype == np.float32
+    b = nx.check_image(np.zeros((2, 3, 4), dtype=np.float64))
+    assert b.shape == (2, 3, 4) and b.dtype == np.float32
+    with pytest.raises(ValueError):
+        nx.check_image(np.zeros(5))
+    with pytest.raises(ValueError):
+        nx.check_image(np.zeros((1, 2, 3, 4)))
+    t = nx.check_image(torch.zeros(3, 4, dtype=torch.float64))
+    assert tuple(t.shape) == (1, 3, 4) and t.dtype == torch.float32
+
+
+def test_value2array():
+    assert np.array_equal(nx.value2array(1.5, 3), np.full(3, 1.5, np.float32))
+    assert nx.value2array(np.array([1, 2]), 2).dtype == np.float32
+
+
+def test_correlation_names_validated_before_any_device_work():
+    with pytest.raises(ValueError, match="AVG, VAR or TAC2"):
+        methods._corr_list("MAX")
+    with pytest.raises(ValueError):
+        methods._corr_list([])
+    assert methods._corr_list(("VAR", "TAC2")) == ["VAR", "TAC2"]
+
+
+def test_unimplemented_options_raise():
+    with pytest.raises(NotImplementedError):
+        nx.eSRRF(np.zeros((2, 4, 4), np.float32), use_fht=True)
+    with pytest.raises(NotImplementedError):
+        nx.run_esrrf_parameter_sweep(np.zeros((2, 4, 4), np.float32))
+
+
+class _Add(LiquidEngine):
+    def run(self, a, b, run_type=None):
+        return self._run(a, b, run_type=run_type)
+
+    def _run_cuda(self, a, b):
+        return a + b
+
+
+class _Split(LiquidEngine):
+    def run(self, a, run_type=None):
+        return self._run(a, run_type=run_type)
+
+    def _run_cuda(self, a):
+        return a, 2 * a
+
+
+def test_workflow_prev_return_value_wiring():
+    wf = nx.Workflow((_Split(), (np.array([1.0]),), {}),
+                     (_Add(), ("PREV_RETURN_VALUE_0_0", "PREV_RETURN_VALUE_0_1"), {}))
+    out = wf.calculate()
+    assert np.array_equal(out[0], np.array([3.0]))
+    with pytest.raises(TypeError):
+        nx.Workflow((1, 2))
+
+
+def test_synthetic_generator_deterministic_and_plausible():
+    a = synthetic.blinking_stack(20, 32, 40, 10, seed=3)
+    b = synthetic.blinking_stack(20, 32, 40, 10, seed=3)
+    c = synthetic.blinking_stack(20, 32, 40, 10, seed=4)
+    assert a.dtype == np.float32 and a.shape == (20, 32, 40) and a.flags.c_contiguous
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    # background 100 photons/px: median close to 100
+    assert 95 < float(np.median(a)) < 106
+    assert synthetic.emitters_for_density(100, 100, 0.006) == 60

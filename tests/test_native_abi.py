@@ -1,0 +1,82 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares.
+
+No compute call is made here (no GPU needed); the host-only weight-table entry
+point is checked against an independent NumPy evaluation of the reference's
+distance weight (_c_sr_radial_gradient_convergence.c:4-6).
+"""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from nanopyx_gb300 import _build, _native
+
+
+def _declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(nx_\w+)\s*\(", src))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_build.LIB):
+        _build.build()
+    return _native.lib()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = _declared_symbols()
+    assert len(declared) >= 20
+    raw = ctypes.CDLL(_build.LIB)
+    missing = [n for n in declared if not hasattr(raw, n)]
+    assert not missing, missing
+    assert sorted(_native.exported_symbols()) == declared
+
+
+def test_abi_version(lib):
+    assert lib.nx_abi_version() == 1
+
+
+def _weights_numpy(m, radius):
+    sigma = np.float32(radius / 2.355)
+    tSS = np.float32(np.float32(2) * sigma * sigma)
+    tSO = np.float32(np.float32(2) * sigma + np.float32(1))
+    J = int(np.float32(2.0) * np.float32(radius))
+    W2 = 2 * J + 1
+    out = np.zeros((m, m, W2, W2))
+    for py in range(m):
+        cy = (2 * py + 1) // m
+        for px in range(m):
+            cx = (2 * px + 1) // m
+            for jj in range(W2):
+                dy = (cy + jj - J) / 2 - (py + 0.5) / m
+                for ii in range(W2):
+                    dx = (cx + ii - J) / 2 - (px + 0.5) / m
+                    d = float(np.float32(np.hypot(dx, dy)))
+                    if d != 0 and d <= tSO:
+                        out[py, px, jj, ii] = (d * np.exp(-d * d / float(tSS))) ** 4
+    return J, out
+
+
+@pytest.mark.parametrize("m,radius", [(5, 1.5), (2, 1.0), (4, 2.5), (3, 1.25)])
+def test_weight_table_matches_numpy(lib, m, radius):
+    J, ref = _weights_numpy(m, radius)
+    buf = np.zeros(ref.size, dtype=np.float32)
+    got_J = lib.nx_esrrf_weight_table(m, radius, buf.ctypes.data, buf.size)
+    assert got_J == J
+    got = buf.reshape(ref.shape)
+    assert np.allclose(got, ref, rtol=2e-7, atol=0)
+
+
+def test_weight_table_rejects_bad_args(lib):
+    assert lib.nx_esrrf_weight_table(0, 1.5, None, 0) == _native.NX_ERR_INVALID_ARG
+    assert lib.nx_esrrf_weight_table(5, -1.0, None, 0) == _native.NX_ERR_INVALID_ARG
+    assert "radius" in lib.nx_last_error().decode()

@@ -1,0 +1,86 @@
+"""Pin the FP64 oracle (oracle/esrrf_np.py) against the reference's own outputs.
+
+The golden vectors were produced by the reference's compiled Cython path
+(tests/golden/make_golden.py); the oracle is accepted only if it reproduces
+every one of them within the parity bar of this path (1e-4 of the output range;
+observed ~1e-6 at these sizes -- the difference is the reference's float32
+rounding of its sampling coordinates).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import esrrf_np as O
+from oracle import ref_build
+
+TOL = 1e-4
+
+
+def test_oracle_esrrf_st(golden):
+    x = golden["esrrf_st/input"]
+    for k, (m, r, s, iw) in enumerate(golden["esrrf_st/cases"]):
+        got = O.esrrf_st(x, int(m), float(r), float(s), bool(iw))
+        assert rel_err(got, golden[f"esrrf_st/{k}"]) <= TOL, (k, m, r, s, iw)
+
+
+@pytest.mark.parametrize("corr", ["AVG", "VAR", "TAC2"])
+@pytest.mark.parametrize("mpc", [0, 1])
+def test_oracle_esrrf_full(golden, corr, mpc):
+    x = golden["esrrf/input"]
+    got = O.esrrf(x, 5, 1.5, 2, 5, corr, True, bool(mpc))
+    assert rel_err(got, golden[f"esrrf/{corr}/{mpc}"]) <= TOL
+
+
+def test_oracle_cr_and_robx(golden):
+    x = golden["cr/input"]
+    assert rel_err(O.cr_shift_magnify(x, 0, 0, 5, 5), golden["cr/0"]) <= 1e-6
+    assert rel_err(O.cr_shift_magnify(x, 0.3, -1.2, 2.5, 3.0), golden["cr/1"]) <= 1e-6
+    assert rel_err(O.cr_shift_magnify(x, 0, 0, 10, 10), golden["cr/2"]) <= 1e-6
+    gc, gr = O.roberts_cross(x)
+    # float64 restatement vs the reference's float32 sums: equal to float32 rounding
+    assert rel_err(gc, golden["robx/gc"]) <= 1e-6
+    assert rel_err(gr, golden["robx/gr"]) <= 1e-6
+
+
+def test_oracle_rgc_standalone(golden):
+    gci, gri, mag = golden["rgc/gci"], golden["rgc/gri"], golden["rgc/mag"]
+    assert rel_err(O.radial_gradient_convergence(gci, gri, mag, 4, 1.5, 1), golden["rgc/0"]) <= TOL
+    assert rel_err(O.radial_gradient_convergence(gci, gri, mag, 4, 1.5, 2, True, True),
+                   golden["rgc/1"]) <= TOL
+    assert rel_err(O.radial_gradient_convergence(gci, gri, mag, 4, 2.0, 1, False),
+                   golden["rgc/2"]) <= TOL
+
+
+def test_oracle_radiality(golden):
+    x = golden["srrf/input"]
+    for k, (m, ring, border, pos) in enumerate([(5, 0.5, 0, True), (4, 1.0, 1, False),
+                                                 (2, 0.5, 0, True)]):
+        mag = O.cr_shift_magnify(x, 0, 0, m, m)
+        got = O.radiality(x, mag, m, ring, border, pos)
+        assert rel_err(got, golden[f"srrf/{k}"]) <= TOL, k
+        assert rel_err(O.macro_pixel_correct(got, m), golden[f"srrf/{k}/mpc"]) <= TOL, k
+
+
+def test_oracle_temporal_and_mpc(golden):
+    x = golden["temporal/input"]
+    for corr in ("AVG", "VAR", "TAC2"):
+        assert rel_err(O.temporal_correlation(x, corr), golden[f"temporal/{corr}"]) <= 1e-5
+    x = golden["mpc/input"]
+    assert rel_err(O.macro_pixel_correct(x, 5), golden["mpc/5"]) <= 1e-5
+
+
+def test_oracle_rejects_bad_correlation():
+    with pytest.raises(ValueError):
+        O.temporal_correlation(np.zeros((2, 3, 3)), "MAX")
+
+
+def test_compiled_reference_reproduces_golden(golden):
+    if not ref_build.available():
+        pytest.skip("oracle/_ref not built on this machine")
+    R = ref_build.load()
+    x = golden["esrrf_st/input"]
+    for k, (m, r, s, iw) in enumerate(golden["esrrf_st/cases"][:4]):
+        out = R["eSRRF_ST"](verbose=False).run(x, magnification=int(m), radius=float(r),
+                                               sensitivity=float(s), doIntensityWeighting=bool(iw),
+                                               run_type="Threaded")
+        assert rel_err(out, golden[f"esrrf_st/{k}"]) <= 1e-5
