@@ -36,12 +36,14 @@ if ROOT not in sys.path:
 
 CFG = dict(T=500, H=512, W=512, emitters=400, m=5, radius=1.5, sensitivity=2.0,
            correlations=("VAR", "TAC2"), fpt=100, mpc=True, seed=1)
+# profiling case: same kernel and frame size, 160 frames (168 MB input, still > L2)
+SMALL = dict(T=160, fpt=80)
 METRIC = "eSRRF input Mpx*frames/s"
 REF_SAMPLE_FRAMES = 4
 
 
 def _workload_name():
-    return (f"large single eSRRF {CFG['T']}x{CFG['H']}x{CFG['W']} m={CFG['m']} R={CFG['radius']} "
+    return (f"single eSRRF {CFG['T']}x{CFG['H']}x{CFG['W']} m={CFG['m']} R={CFG['radius']} "
             f"s={CFG['sensitivity']:g} VAR+TAC2 fpt={CFG['fpt']} MPC")
 
 
@@ -363,7 +365,7 @@ def run_gpu_arm(args):
                    "radius": R, "sensitivity": s, "correlations": list(CFG["correlations"]),
                    "frames_per_timepoint": fpt, "macro_pixel_correction": True,
                    "parallelism": f"replicas{world}" if world > 1 else "single GPU",
-                   "l2": "input 524 MB > 129 MB L2; no flush"},
+                   "l2": f"input {stack_np.nbytes / 1e6:.0f} MB > 129 MB L2; no flush"},
         "e2e": {"value": mpxf / e2e_s, "unit": "Mpx*frames/s", "seconds": e2e_s,
                 "h2d_bytes_per_step": int(stack_np.nbytes), "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": args.steps * (1 + n_tp + 2),
@@ -390,7 +392,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="large", choices=["large", "small"],
+                    help="small: 160 frames, 80 per timepoint (for ncu captures)")
     args = ap.parse_args()
+    if args.workload == "small":
+        CFG.update(SMALL)
     if args.impl == "reference":
         return run_reference_arm(args)
     return run_gpu_arm(args)
