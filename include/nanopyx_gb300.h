@@ -167,6 +167,18 @@ size_t nx_macro_pixel_workspace_bytes(int S, int magnification);
 int nx_macro_pixel_correct(float* d_img, int S, int rowsM, int colsM, int magnification,
                            void* d_ws, size_t ws_bytes, void* stream);
 
+/* Macro-pixel correction that allocates nothing -- no counterpart in the
+ * reference.  For callers that may not allocate device memory while they run
+ * (real-time acquisition loops that reserve everything at start-up, hosts whose
+ * own allocator owns the GPU): same result as nx_macro_pixel_correct, with the
+ * scratch in a 256 KiB device array owned by the library (held on every GPU
+ * that loads it, until exit).  Calls needing more scratch than that
+ * (nx_macro_pixel_workspace_bytes(S, m) > 262144) return NX_ERR_INVALID_ARG.
+ * The first call on a device resolves the array's address and must come
+ * before any stream capture; calls that overlap on the GPU race on the array. */
+int nx_macro_pixel_correct_static(float* d_img, int S, int rowsM, int colsM, int magnification,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

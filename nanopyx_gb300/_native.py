@@ -71,6 +71,7 @@ _SIGS = {
     "nx_srrf_temporal_correlation": (_I, [_P, _I, _LL, _I, _P, _P]),
     "nx_macro_pixel_workspace_bytes": (_SZ, [_I, _I]),
     "nx_macro_pixel_correct": (_I, [_P, _I, _I, _I, _I, _P, _SZ, _P]),
+    "nx_macro_pixel_correct_static": (_I, [_P, _I, _I, _I, _I, _P]),
 }
 
 _lib = None
