@@ -94,6 +94,8 @@ int nx_esrrf_run_stage2(const nx_esrrf_plan* plan, int T, int frames_per_timepoi
  * d_sink (blocks*256 floats) so nothing is optimised away.  Used to measure
  * the FP32 FMA peak the RGC kernel is compared against.                       */
 int nx_probe_ffma(float* d_sink, int blocks, int iters, void* stream);
+/* Same work with Blackwell's packed FP32 FMA (f32x2): 4 chains of 2 lanes.   */
+int nx_probe_ffma2(float* d_sink, int blocks, int iters, void* stream);
 
 /* Streaming accumulation for served requests: frame blocks of one
  * reconstruction are pushed as they arrive; the device-resident accumulator

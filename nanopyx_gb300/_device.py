@@ -90,8 +90,12 @@ def stream_ptr(device=None) -> int:
 
 
 def workspace(nbytes: int, device=None) -> torch.Tensor:
+    """Device scratch for one C-ABI call; its first 256 bytes (the device status
+    word the kernels report bounded-wait timeouts into) start at zero."""
     device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
-    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    ws = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+    ws[:256].zero_()
+    return ws
 
 
 class _Plan:

@@ -57,6 +57,7 @@ _SIGS = {
     "nx_esrrf_run_stage1": (_I, [_P, _P, _I, _I, _I, _P, _SZ, _P]),
     "nx_esrrf_run_stage2": (_I, [_P, _I, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_probe_ffma": (_I, [_P, _I, _I, _P]),
+    "nx_probe_ffma2": (_I, [_P, _I, _I, _P]),
     "nx_esrrf_accum_bytes": (_SZ, [_P]),
     "nx_esrrf_push_workspace_bytes": (_SZ, [_P, _I]),
     "nx_esrrf_accum_push": (_I, [_P, _P, _I, _I, _P, _P, _SZ, _P]),

@@ -164,7 +164,7 @@ static void build_tables(nx_esrrf_plan* p, std::vector<float>& tbl, std::vector<
   tbl.assign((size_t)M * W2 * 3 * NS4 * 4, 0.f);
   inv.assign((size_t)M * M, 0.f);
   wfull.assign((size_t)M * M * W2 * W2, 0.f);
-  const double tSS = p->sc.tSS, tSO = p->sc.tSO;
+  const double tSS = p->sc.tSS;
   std::vector<double> wsum((size_t)M * M, 0.0);
   for (int py = 0; py < M; ++py) {
     const int cpy = (2 * py + 1) / M;
@@ -189,7 +189,6 @@ static void build_tables(nx_esrrf_plan* p, std::vector<float>& tbl, std::vector<
             a = (float)(dx * wd);
             b = (float)(dy * wd);
           }
-          (void)tSO;
           const int sidx = px * W2 + ii;
           blk[0 * NS4 * 4 + sidx] = a;
           blk[1 * NS4 * 4 + sidx] = b;
@@ -460,7 +459,7 @@ size_t nx_esrrf_workspace_bytes(const nx_esrrf_plan* p, int T, int fpt, int corr
     b += align256((size_t)n_tp * 5 * planeM * sizeof(float));
     b += align256(generic_frame_floats(p) * sizeof(float));
   }
-  b += align256((size_t)corr_count(corr_mask) * n_tp * p->M * p->M * sizeof(float));
+  b += nx_macro_pixel_workspace_bytes(corr_count(corr_mask) * n_tp, p->M);
   return b;
 }
 
@@ -623,7 +622,7 @@ int nx_esrrf_accum_finalize(const nx_esrrf_plan* p, const void* d_accum, int tot
   if (total_frames < 1) return invalid("no frames were pushed");
   if (corr_mask <= 0 || corr_mask > 7) return invalid("Type of correlation must be AVG, VAR or TAC2");
   const int ncorr = corr_count(corr_mask);
-  const size_t need = kStatusBytes + align256((size_t)ncorr * p->M * p->M * sizeof(float));
+  const size_t need = kStatusBytes + nx_macro_pixel_workspace_bytes(ncorr, p->M);
   if (!d_ws || ws_bytes < need) {
     set_error("workspace too small: need %zu bytes", need);
     return NX_ERR_WORKSPACE;
@@ -737,7 +736,8 @@ int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n, int o
 }
 
 size_t nx_macro_pixel_workspace_bytes(int S, int magnification) {
-  return align256((size_t)std::max(S, 1) * magnification * magnification * sizeof(float));
+  return align256((size_t)std::max(S, 1) * magnification * magnification * kMpcChunks *
+                  sizeof(float));
 }
 
 int nx_macro_pixel_correct(float* d_img, int S, int rowsM, int colsM, int magnification,

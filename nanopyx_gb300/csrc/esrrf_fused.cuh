@@ -106,7 +106,10 @@ struct Geo {
   static constexpr int S_RW = al(OY * 5);
   static constexpr int O_CW = O_RW + S_RW;
   static constexpr int S_CW = al(OX * 5);
-  static constexpr int O_BAR = O_CW + S_CW;
+  // per-thread constants / state kept out of registers: [px][thread]
+  static constexpr int O_TW = O_CW + S_CW;   // 1 / sum w per output
+  static constexpr int O_TK = O_TW + M * NT; // temporal shift K per output
+  static constexpr int O_BAR = O_TK + M * NT;
   static constexpr int FLOATS = O_BAR + 32;
   static constexpr size_t SMEM_BYTES = size_t(FLOATS) * 4;
 };
@@ -116,7 +119,7 @@ __device__ __forceinline__ float f4c(const float4& v, int e) {
 }
 
 template <int M, int J, int TY, int MODE>
-__global__ void __launch_bounds__(32 * TY * M, 1)
+__global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     esrrf_fused_kernel(const __grid_constant__ CUtensorMap tmap, const FusedParams p) {
   using G = Geo<M, J, TY>;
   constexpr int F = mode_fields(MODE);
@@ -131,6 +134,8 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
   float* rw = sm + G::O_RW;
   float* cw = sm + G::O_CW;
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + G::O_BAR);
+  float* tw = sm + G::O_TW;  // tw[px * NT + tid]
+  float* tk = sm + G::O_TK;  // tk[px * NT + tid]
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -209,7 +214,6 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
   const int nx = nx0 + lane;
   const int yM = ny * M + py;
   const int cpy = (2 * py + 1) / M;
-  float inv_w[M];
   unsigned omask = 0;  // bit px: output forced to 0 / not written
   {
     const int ky_lo = 2 * ny + cpy - J, ky_hi = 2 * ny + cpy + J;
@@ -235,7 +239,7 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
         }
         iw = s > 0.f ? 1.f / s : 0.f;
       }
-      inv_w[px] = iw;
+      tw[px * G::NT + tid] = iw;
       const bool outside = (ny >= H) || (nx >= W);
       const bool in_margin = (yM < p.margin) || (yM >= p.rowsM - p.margin) ||
                              (xM < p.margin) || (xM >= p.colsM - p.margin);
@@ -244,10 +248,10 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
     }
   }
 
-  float accK[M], accS[M], accQ[M], accP[M], accL[M];
+  float accS[M], accQ[M], accP[M], accL[M];
 #pragma unroll
   for (int px = 0; px < M; ++px) {
-    accK[px] = 0.f; accS[px] = 0.f; accQ[px] = 0.f; accP[px] = 0.f; accL[px] = 0.f;
+    accS[px] = 0.f; accQ[px] = 0.f; accP[px] = 0.f; accL[px] = 0.f;
   }
 
   constexpr unsigned kTileBytes = unsigned(G::BH * G::BW * 4);
@@ -415,6 +419,8 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
     __syncthreads();
 
     // ---- phase 4: RGC for this thread's M outputs --------------------------
+    // contribution of sample (phase, offset): (dp < 0) ? w - |u| : 0 with
+    // dp = n.(a, b) and u = n x (a, b) (n the unit gradient)
     float acc[M];
 #pragma unroll
     for (int px = 0; px < M; ++px) acc[px] = 0.f;
@@ -454,7 +460,7 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
     const float* irow = inten + (ty * M + py) * G::OX + lane * M;
 #pragma unroll
     for (int px = 0; px < M; ++px) {
-      float r = acc[px] * inv_w[px];
+      float r = acc[px] * tw[px * G::NT + tid];
       r = (r < 0.f) ? 0.f : r;
       if (p.sens_mode == 1) {
         const float base = r;
@@ -467,8 +473,8 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
       if (MODE == kModeStack) {
         if (!(omask >> 31)) p.out[(size_t)f * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
       } else {
-        if (it == 0) accK[px] = r;
-        const float y = r - accK[px];
+        if (it == 0) tk[px * G::NT + tid] = r;
+        const float y = r - tk[px * G::NT + tid];
         accS[px] += y;
         if (MODE == kModeFull) {
           accQ[px] = fmaf(y, y, accQ[px]);
@@ -496,7 +502,7 @@ __global__ void __launch_bounds__(32 * TY * M, 1)
                  (size_t)nx * M;
 #pragma unroll
     for (int px = 0; px < M; ++px) {
-      rec[px] = accK[px];
+      rec[px] = tk[px * G::NT + tid];
       rec[plane + px] = accS[px];
       if (MODE == kModeFull) {
         rec[2 * plane + px] = accQ[px];
@@ -519,6 +525,9 @@ cudaError_t launch_fused(const FusedParams& p, const CUtensorMap& tmap, cudaStre
   if (attr_done != dev) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)G::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     attr_done = dev;
   }

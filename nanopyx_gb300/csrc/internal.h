@@ -72,7 +72,8 @@ cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int co
                                   cudaStream_t s);
 cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int order, float* out,
                                  cudaStream_t s);
-// macro-pixel correction of S images in place; map scratch holds S*M*M floats
+// macro-pixel correction of S images in place; scratch holds S*M*M*kMpcChunks floats
+constexpr int kMpcChunks = 64;
 cudaError_t launch_mpc(float* img, int S, int rowsM, int colsM, int M, float* map,
                        cudaStream_t s);
 

@@ -4,6 +4,7 @@
 // These follow the reference's float32 arithmetic per output pixel (they are
 // the drop-ins for the individual ops and the general fallback of the fused
 // kernel); the fused frame-loop kernel in esrrf_fused.cuh is the hot path.
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -419,17 +420,21 @@ __global__ void srrf_temporal_kernel(const float* __restrict__ x, int T, long lo
   }
 }
 
-// macro-pixel map: block (s, py); thread t sums phase px = t % M over its
-// columns and all macro-pixel rows (Kahan); fixed-order block reduction
-__global__ void mpc_map_kernel(const float* __restrict__ img, int rowsM, int colsM, int M,
-                               float* __restrict__ map) {
+// macro-pixel map, stage 1: block (s, py, chunk) sums the macro-pixel rows
+// [chunk*rpc, (chunk+1)*rpc) of phase row py; thread t owns phase px = t % M
+// (blockDim is a multiple of M); Kahan sums, fixed-order block reduction.
+__global__ void mpc_partial_kernel(const float* __restrict__ img, int rowsM, int colsM, int M,
+                                   int nch, float* __restrict__ part) {
   extern __shared__ float red[];
   const int s = blockIdx.x;
   const int py = blockIdx.y;
+  const int ch = blockIdx.z;
   const int rows = rowsM / M, cols = colsM / M;
+  const int rpc = (rows + nch - 1) / nch;
+  const int r0 = ch * rpc, r1 = min(rows, r0 + rpc);
   const float* f = img + (size_t)s * rowsM * colsM;
   float sum = 0.f, comp = 0.f;
-  for (int ry = 0; ry < rows; ++ry) {
+  for (int ry = r0; ry < r1; ++ry) {
     const float* row = f + (size_t)(ry * M + py) * colsM;
     for (int x = threadIdx.x; x < cols * M; x += blockDim.x) {
       const float yk = row[x] - comp;
@@ -448,22 +453,39 @@ __global__ void mpc_map_kernel(const float* __restrict__ img, int rowsM, int col
       c2 = (tk - tot) - yk;
       tot = tk;
     }
-    map[(size_t)s * M * M + py * M + threadIdx.x] = tot / (float)(rows * cols);
+    part[(((size_t)s * M + py) * nch + ch) * M + threadIdx.x] = tot;
   }
 }
 
-__global__ void mpc_apply_kernel(float* __restrict__ img, int S, int rowsM, int colsM, int M,
-                                 const float* __restrict__ map) {
+// stage 2: every block rebuilds its slice's M x M map from the partials (fixed
+// order) and divides its pixels by the map value of their phase when non-zero.
+__global__ void mpc_apply_kernel(float* __restrict__ img, int rowsM, int colsM, int M, int nch,
+                                 const float* __restrict__ part) {
+  extern __shared__ float cmap[];
+  const int s = blockIdx.y;
+  const int rows = rowsM / M, cols = colsM / M;
+  const float inv_n = 1.f / (float)((long long)rows * cols);
+  for (int k = threadIdx.x; k < M * M; k += blockDim.x) {
+    const int py = k / M, px = k % M;
+    const float* pp = part + ((size_t)s * M + py) * nch * M + px;
+    float tot = 0.f, c2 = 0.f;
+    for (int ch = 0; ch < nch; ++ch) {
+      const float yk = pp[(size_t)ch * M] - c2;
+      const float tk = tot + yk;
+      c2 = (tk - tot) - yk;
+      tot = tk;
+    }
+    cmap[k] = (rows * cols > 0) ? tot * inv_n : 0.f;
+  }
+  __syncthreads();
   const long long plane = (long long)rowsM * colsM;
-  const long long n = plane * S;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+  float* f = img + (size_t)s * plane;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < plane;
        idx += (long long)gridDim.x * blockDim.x) {
-    const int s = (int)(idx / plane);
-    const long long rem = idx - (long long)s * plane;
-    const int yM = (int)(rem / colsM);
-    const int xM = (int)(rem - (long long)yM * colsM);
-    const float c = map[(size_t)s * M * M + (yM % M) * M + (xM % M)];
-    if (c != 0.f) img[idx] = __fdiv_rn(img[idx], c);
+    const int yM = (int)(idx / colsM);
+    const int xM = (int)(idx - (long long)yM * colsM);
+    const float c = cmap[(yM % M) * M + (xM % M)];
+    if (c != 0.f) f[idx] = __fdiv_rn(f[idx], c);
   }
 }
 
@@ -590,13 +612,22 @@ cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int ord
 cudaError_t launch_mpc(float* img, int S, int rowsM, int colsM, int M, float* map,
                        cudaStream_t s) {
   if ((long long)S * rowsM * colsM == 0) return cudaSuccess;
+  const int rows = rowsM / M;
+  const int nch = std::max(1, std::min(kMpcChunks, rows));
   const int block = M <= 32 ? 32 * M : ((1024 / M) * M);
-  mpc_map_kernel<<<dim3((unsigned)S, (unsigned)M), block, block * sizeof(float), s>>>(
-      img, rowsM, colsM, M, map);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  const long long n = (long long)S * rowsM * colsM;
-  mpc_apply_kernel<<<grid_for(n), kBlock, 0, s>>>(img, S, rowsM, colsM, M, map);
+  if (rows > 0) {
+    mpc_partial_kernel<<<dim3((unsigned)S, (unsigned)M, (unsigned)nch), block,
+                         block * sizeof(float), s>>>(img, rowsM, colsM, M, nch, map);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  } else {
+    cudaError_t e = cudaMemsetAsync(map, 0, (size_t)S * M * M * nch * sizeof(float), s);
+    if (e != cudaSuccess) return e;
+  }
+  const long long plane = (long long)rowsM * colsM;
+  unsigned gx = (unsigned)std::min<long long>((plane + 1023) / 1024, 4096);
+  mpc_apply_kernel<<<dim3(gx, (unsigned)S), 256, (size_t)M * M * sizeof(float), s>>>(
+      img, rowsM, colsM, M, nch, map);
   return cudaGetLastError();
 }
 

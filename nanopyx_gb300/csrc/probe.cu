@@ -17,7 +17,29 @@ __global__ void __launch_bounds__(256) ffma_probe_kernel(float* sink, int iters)
   sink[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+__global__ void __launch_bounds__(256) ffma2_probe_kernel(float* sink, int iters) {
+  float2 a0 = make_float2(threadIdx.x * 1e-3f, 1.f), a1 = make_float2(2.f, 3.f);
+  float2 a2 = make_float2(4.f, 5.f), a3 = make_float2(6.f, 7.f);
+  const float2 b = make_float2(0.999f, 0.999f), c = make_float2(1e-4f, 1e-4f);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      a0 = __ffma2_rn(a0, b, c); a1 = __ffma2_rn(a1, b, c);
+      a2 = __ffma2_rn(a2, b, c); a3 = __ffma2_rn(a3, b, c);
+    }
+  }
+  sink[blockIdx.x * blockDim.x + threadIdx.x] =
+      a0.x + a0.y + a1.x + a1.y + a2.x + a2.y + a3.x + a3.y;
+}
+
 }  // namespace
+
+extern "C" int nx_probe_ffma2(float* d_sink, int blocks, int iters, void* stream) {
+  if (!d_sink || blocks < 1 || iters < 1) return NX_ERR_INVALID_ARG;
+  ffma2_probe_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(d_sink, iters);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NX_OK : nx::cuda_status(e, "ffma2 probe");
+}
 
 extern "C" int nx_probe_ffma(float* d_sink, int blocks, int iters, void* stream) {
   if (!d_sink || blocks < 1 || iters < 1) return NX_ERR_INVALID_ARG;

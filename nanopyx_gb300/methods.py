@@ -20,7 +20,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from ._device import get_plan, stream_ptr, to_device_stack, workspace
+from ._device import check_image, get_plan, stream_ptr, to_device_stack, workspace
 from .transform import (GradientRobertsCross, Radiality, ShiftAndMagnify,  # noqa: F401
                         macro_pixel_corrector)
 
@@ -86,15 +86,96 @@ def eSRRF(image, magnification: int = 5, radius: float = 1.5, sensitivity: float
     if use_fht:
         raise NotImplementedError("use_fht=True (Fourier interpolation) is not implemented")
     names = _corr_list(temporal_correlation)
-    st = to_device_stack(image)
-    out = esrrf_device(st.t, magnification, radius, sensitivity, frames_per_timepoint, names,
-                       doIntensityWeighting, macro_pixel_correction)
-    res = st.out(out)
-    if st.from_numpy:
-        parts = [np.squeeze(res[i].astype(np.float32)) for i in range(len(names))]
+    if isinstance(image, torch.Tensor) and image.is_cuda:
+        st = to_device_stack(image)
+        out = esrrf_device(st.t, magnification, radius, sensitivity, frames_per_timepoint,
+                           names, doIntensityWeighting, macro_pixel_correction)
+        parts = [torch.squeeze(out[i]) for i in range(len(names))]
     else:
-        parts = [torch.squeeze(res[i]) for i in range(len(names))]
+        img = check_image(image.numpy() if isinstance(image, torch.Tensor) else image)
+        res = _esrrf_host(np.ascontiguousarray(img), magnification, radius, sensitivity,
+                          frames_per_timepoint, names, doIntensityWeighting,
+                          macro_pixel_correction)
+        parts = [np.squeeze(res[i]) for i in range(len(names))]
     return parts[0] if isinstance(temporal_correlation, str) else tuple(parts)
+
+
+def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_timepoint,
+                names, doIntensityWeighting, macro_pixel_correction) -> np.ndarray:
+    """eSRRF with host buffers, copies overlapped with compute.
+
+    The stack is uploaded in segments on a copy stream (a timepoint, or a
+    quarter of it when there are fewer than three timepoints); each segment is
+    folded into its timepoint's device-resident accumulator on the compute
+    stream while the next one uploads, and each finished timepoint is copied
+    back while the next computes.  Same arithmetic as ``esrrf_device``.
+    Returns (n_corr, n_timepoints, H*m, W*m) float32.
+    """
+    from ._device import require_cuda
+
+    dev = require_cuda()
+    T, H, W = arr.shape
+    if T < 1:
+        raise ValueError("eSRRF needs at least one frame")
+    fpt = T if frames_per_timepoint == 0 or frames_per_timepoint > T else int(frames_per_timepoint)
+    if fpt < 0:
+        raise ValueError("frames_per_timepoint must be >= 0")
+    n_tp = T // fpt + (1 if T % fpt else 0)
+    m = int(magnification)
+    mask = 0
+    for n in names:
+        mask |= N.CORR_BITS[n]
+    order = [b for b in ("AVG", "VAR", "TAC2") if mask & N.CORR_BITS[b]]
+    sel = [order.index(n) for n in names]
+    L = N.lib()
+    plan = get_plan(H, W, m, radius, sensitivity, doIntensityWeighting)
+    comp = torch.cuda.current_stream(dev)
+    cp = torch.cuda.Stream(dev)
+    nseg = 1 if n_tp >= 3 else min(4, fpt)
+    seg_len = -(-fpt // nseg)
+    max_seg = min(seg_len, T)
+    ws_push = workspace(L.nx_esrrf_push_workspace_bytes(plan.handle, max_seg), dev)
+    ws_fin = workspace(256 + L.nx_macro_pixel_workspace_bytes(3, m), dev)
+    acc = [torch.empty(L.nx_esrrf_accum_bytes(plan.handle), dtype=torch.uint8, device=dev)
+           for _ in range(2)]
+    outs = [torch.empty((len(order), H * m, W * m), dtype=torch.float32, device=dev)
+            for _ in range(2)]
+    res = np.empty((len(names), n_tp, H * m, W * m), dtype=np.float32)
+    done = [None, None]
+
+    def drain(tp):
+        k = tp & 1
+        cp.wait_event(done[k])
+        with torch.cuda.stream(cp):
+            host = outs[k].cpu()
+        res[:, tp] = host.numpy()[sel]
+
+    pending = None
+    for tp in range(n_tp):
+        a0, a1 = tp * fpt, min(T, (tp + 1) * fpt)
+        k = tp & 1
+        before = 0
+        for sa in range(a0, a1, seg_len):
+            sb = min(a1, sa + seg_len)
+            with torch.cuda.stream(cp):
+                seg = torch.from_numpy(arr[sa:sb]).to(dev, non_blocking=True)
+            comp.wait_stream(cp)
+            seg.record_stream(comp)
+            N.check(L.nx_esrrf_accum_push(plan.handle, seg.data_ptr(), sb - sa, before,
+                                          acc[k].data_ptr(), ws_push.data_ptr(), ws_push.numel(),
+                                          comp.cuda_stream), "eSRRF push")
+            before += sb - sa
+        if pending is not None:
+            drain(pending)  # outs[pending & 1] is free again after this
+        N.check(L.nx_esrrf_accum_finalize(plan.handle, acc[k].data_ptr(), before, mask,
+                                          1 if macro_pixel_correction else 0,
+                                          outs[k].data_ptr(), ws_fin.data_ptr(),
+                                          ws_fin.numel(), comp.cuda_stream), "eSRRF finalize")
+        done[k] = comp.record_event()
+        pending = tp
+    drain(pending)
+    N.check(L.nx_workspace_status(ws_push.data_ptr(), comp.cuda_stream), "eSRRF")
+    return res
 
 
 def SRRF(image, magnification: int = 5, ringRadius: float = 0.5, border: int = 0,
@@ -232,7 +313,7 @@ class ESRRFAccumulator:
         out = torch.empty((len(order), self.H * self.m, self.W * self.m), dtype=torch.float32,
                           device=self.device)
         L = N.lib()
-        ws = self._workspace(256 + 4 * 3 * self.m * self.m + 256)
+        ws = self._workspace(256 + L.nx_macro_pixel_workspace_bytes(3, self.m))
         N.check(L.nx_esrrf_accum_finalize(self.plan.handle, self.state.data_ptr(), self.frames,
                                           mask, 1 if macro_pixel_correction else 0,
                                           out.data_ptr(), ws.data_ptr(), ws.numel(),
