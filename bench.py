@@ -375,7 +375,8 @@ def run_gpu_arm(args):
         "gpu_launches": args.steps * (1 + n_tp + 2),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "esrrf_fused_kernel<5,3,2,FULL>", "kernel_ms": kern_ms,
+                     "kernel": f"esrrf_fused_kernel<m={m},J={int(2 * R)},FULL>",
+                     "kernel_ms": kern_ms,
                      "flops_per_launch": flops, "samples_per_output": S,
                      "peak_scalar_ffma": peak_scalar, "peak_packed_ffma2": peak_packed,
                      "peak_source": "measured FMA-loop throughput on this GPU, best of scalar FFMA "

@@ -112,6 +112,37 @@ int nx_esrrf_accum_finalize(const nx_esrrf_plan* plan, const void* d_accum, int 
                             int corr_mask, int macro_pixel_correction, float* d_out, void* d_ws,
                             size_t ws_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched eSRRF: many independent reconstructions (uneven H, W, T, m, R,
+ * correlation) and sensitivity sweeps in one persistent launch per kernel
+ * class (m, window), each CTA taking (stack, tile, timepoint, frame chunk)
+ * units from a shared work list.  create() plans the work, bind() uploads the
+ * work lists into the caller's workspace (synchronises `stream`; not
+ * capturable), launch() issues kernels only -- it can be captured into a CUDA
+ * graph and replayed while the buffers stay in place.
+ * Replaces the reference's per-stack loop (eSRRF_workflow.py:76-112) and
+ * the per-(R, s) loop of the parameter sweep (core/analysis/parameter_sweep.py:33-37).
+ * ------------------------------------------------------------------------ */
+typedef struct nx_esrrf_item {
+  const nx_esrrf_plan* plan;   /* H, W, magnification, radius, weighting, sensitivity */
+  const float* d_in;           /* (T, H, W) */
+  int T;
+  int frames_per_timepoint;    /* 0 = all frames */
+  int corr_mask;               /* NX_CORR_*; NX_CORR_AVG when n_sens > 0 */
+  int macro_pixel_correction;
+  int n_sens;                  /* 0: the plan's sensitivity; 1..4: AVG at each of sens[] */
+  float sens[4];
+  int frames_per_unit;         /* frames per work unit (0: heuristic) */
+  float* d_out;                /* (n_corr or n_sens, n_timepoints, H*m, W*m) */
+} nx_esrrf_item;
+
+typedef struct nx_esrrf_batch nx_esrrf_batch;
+int nx_esrrf_batch_create(nx_esrrf_batch** batch, const nx_esrrf_item* items, int n_items);
+size_t nx_esrrf_batch_workspace_bytes(const nx_esrrf_batch* batch);
+int nx_esrrf_batch_bind(nx_esrrf_batch* batch, void* d_ws, size_t ws_bytes, void* stream);
+int nx_esrrf_batch_launch(const nx_esrrf_batch* batch, void* stream);
+int nx_esrrf_batch_destroy(nx_esrrf_batch* batch);
+
 /* Device status word check (synchronises `stream`): returns NX_OK or
  * NX_ERR_DEVICE_TIMEOUT if a kernel of a previous call on this workspace
  * recorded a bounded-wait timeout.                                          */

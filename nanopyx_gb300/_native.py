@@ -28,6 +28,15 @@ NX_CORR_TAC2 = 4
 CORR_BITS = {"AVG": NX_CORR_AVG, "VAR": NX_CORR_VAR, "TAC2": NX_CORR_TAC2}
 
 
+class EsrrfItem(C.Structure):
+    """nx_esrrf_item of include/nanopyx_gb300.h."""
+
+    _fields_ = [("plan", C.c_void_p), ("d_in", C.c_void_p), ("T", C.c_int),
+                ("frames_per_timepoint", C.c_int), ("corr_mask", C.c_int),
+                ("macro_pixel_correction", C.c_int), ("n_sens", C.c_int),
+                ("sens", C.c_float * 4), ("frames_per_unit", C.c_int), ("d_out", C.c_void_p)]
+
+
 class NativeLibraryError(RuntimeError):
     """The CUDA library is missing or failed to load."""
 
@@ -63,6 +72,11 @@ _SIGS = {
     "nx_esrrf_accum_push": (_I, [_P, _P, _I, _I, _P, _P, _SZ, _P]),
     "nx_esrrf_accum_finalize": (_I, [_P, _P, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_workspace_status": (_I, [_P, _P]),
+    "nx_esrrf_batch_create": (_I, [C.POINTER(_P), _P, _I]),
+    "nx_esrrf_batch_workspace_bytes": (_SZ, [_P]),
+    "nx_esrrf_batch_bind": (_I, [_P, _P, _SZ, _P]),
+    "nx_esrrf_batch_launch": (_I, [_P, _P]),
+    "nx_esrrf_batch_destroy": (_I, [_P]),
     "nx_cr_shift_magnify": (_I, [_P, _I, _I, _I, _P, _P, _FL, _FL, _P, _P]),
     "nx_roberts_cross": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "nx_rgc": (_I, [_P, _P, _P, _I, _I, _I, _I, _FL, _FL, _I, _I, _P, _P]),

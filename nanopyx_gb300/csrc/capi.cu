@@ -249,14 +249,16 @@ static void fill_params(const nx_esrrf_plan* p, FusedParams& fp, const float* in
   fp.rowsM = p->rowsM;
   fp.colsM = p->colsM;
   fp.tiles_x = (p->W + 31) / 32;
+  fp.tiles_y = (p->H + p->fused->geo.TY - 1) / p->fused->geo.TY;
   fp.fpt = fpt;
   fp.n_tp = n_tp;
   fp.chunks = chunks;
   fp.margin = p->sc.margin;
   fp.iw = p->iw;
-  fp.sens_mode = p->sc.sens_mode;
-  fp.sens_int = p->sc.sens_int;
-  fp.sens = p->sc.sens;
+  fp.n_sens = 1;
+  fp.sens_mode_k[0] = p->sc.sens_mode;
+  fp.sens_int_k[0] = p->sc.sens_int;
+  fp.sens_k[0] = p->sc.sens;
   fp.cy_base = p->cy_base;
   fp.cx_base = p->cx_base;
   for (int t = 0; t < 4; ++t) {
@@ -268,20 +270,32 @@ static void fill_params(const nx_esrrf_plan* p, FusedParams& fp, const float* in
   fp.wfull = p->d_tbl + p->n_tbl + p->n_inv;
   fp.out = out;
   fp.status = status;
+  fp.tmap = -1;
+  fp.F = 0;
+}
+
+static long long fused_units(const FusedParams& fp) {
+  return (long long)fp.tiles_x * fp.tiles_y * fp.n_tp * fp.chunks;
 }
 
 static int launch_fused_mode(const nx_esrrf_plan* p, int mode, const float* d_in, int T, int fpt,
                              int n_tp, int chunks, float* out, unsigned* status,
                              cudaStream_t s) {
-  FusedParams fp;
-  fill_params(p, fp, d_in, T, fpt, n_tp, chunks, out, status);
-  CUtensorMap tmap;
-  memset(&tmap, 0, sizeof(tmap));
-  fp.use_tma = 0;
-  if (!tma_disabled() && make_frame_tmap(&tmap, d_in, T, p->H, p->W, p->fused->geo.BW,
+  UnitTable ut;
+  memset(&ut, 0, sizeof(ut));
+  fill_params(p, ut.single, d_in, T, fpt, n_tp, chunks, out, status);
+  ut.single.F = mode == kModeFull ? 5 : (mode == kModeSum ? 2 : 0);
+  TmapPack pack;
+  memset(&pack, 0, sizeof(pack));
+  if (!tma_disabled() && make_frame_tmap(&pack.m[0], d_in, T, p->H, p->W, p->fused->geo.BW,
                                          p->fused->geo.BH))
-    fp.use_tma = 1;
-  cudaError_t e = p->fused->launch[mode](fp, tmap, s);
+    ut.single.tmap = 0;
+  const long long units = fused_units(ut.single);
+  if (units > 0x7fffffffLL) return invalid("work too large for one launch");
+  ut.n_items = 1;
+  ut.ns_cap = 1;
+  ut.total_units = (int)units;
+  cudaError_t e = p->fused->launch[mode](ut, pack, ut.total_units, s);
   if (e != cudaSuccess) return cuda_status(e, "fused eSRRF launch");
   return NX_OK;
 }
@@ -357,6 +371,12 @@ int nx_esrrf_plan_create(nx_esrrf_plan** out, int H, int W, int magnification, f
   p->sc = rgc_scalars(magnification, radius, sensitivity, 0);
   p->JW = std::max(-p->sc.start, p->sc.end - 1);
   p->fused = (p->JW >= 1 && p->JW <= 6) ? fused_entry(magnification, p->JW) : nullptr;
+  if (p->fused) {
+    // instantiations whose shared-memory layout does not fit a CTA use the general path
+    const size_t lim = kMaxSmemPerBlock - sizeof(FusedParams) - 64;
+    for (int mode = 0; mode < 3; ++mode)
+      if (p->fused->smem[mode](1) > lim) p->fused = nullptr;
+  }
   clamp_taps(H, magnification, &p->cy_base, p->cy);
   clamp_taps(W, magnification, &p->cx_base, p->cx);
   cudaGetDevice(&p->device);
@@ -537,7 +557,7 @@ int nx_esrrf_run_stage2(const nx_esrrf_plan* p, int T, int fpt, int corr_mask, i
     const int nch = std::min(chunks, nf);
     cudaError_t e = launch_finalize(rec + (size_t)tp * chunks * Fr * planeM, Fr, nch, nf, planeM,
                                     corr_mask, d_out + (size_t)tp * planeM,
-                                    (long long)n_tp * planeM, s);
+                                    (long long)n_tp * planeM, Fr == 5, s);
     if (e != cudaSuccess) return cuda_status(e, "temporal finalize");
   }
   if (mpc) {
@@ -630,13 +650,266 @@ int nx_esrrf_accum_finalize(const nx_esrrf_plan* p, const void* d_accum, int tot
   cudaStream_t s = (cudaStream_t)stream;
   const long long planeM = (long long)p->rowsM * p->colsM;
   cudaError_t e = launch_finalize((const float*)d_accum, 5, 1, total_frames, planeM, corr_mask,
-                                  d_out, planeM, s);
+                                  d_out, planeM, true, s);
   if (e != cudaSuccess) return cuda_status(e, "temporal finalize");
   if (mpc) {
     float* map = (float*)((char*)d_ws + kStatusBytes);
     e = launch_mpc(d_out, ncorr, p->rowsM, p->colsM, p->M, map, s);
     if (e != cudaSuccess) return cuda_status(e, "macro-pixel correction");
   }
+  return NX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct nx_esrrf_batch {
+  struct Item {
+    nx_esrrf_item desc;
+    int mode;            // kModeSum / kModeFull
+    int n_out;           // outputs per timepoint (n_corr or n_sens)
+    int fpt, n_tp, chunks;
+    size_t rec_off;      // byte offsets in the workspace
+    size_t mpc_off;
+    nx::FusedParams fp;  // device pointers filled at bind()
+    int cls;
+  };
+  struct Class {
+    const nx::FusedEntry* entry;
+    int mode;
+    int ns_cap;
+    std::vector<int> items;
+    std::vector<int> unit_start;  // prefix sums, size n + 1
+    size_t params_off, starts_off;
+    int grid;
+    nx::TmapPack maps;
+  };
+  std::vector<Item> items;
+  std::vector<Class> classes;
+  size_t ws_bytes = 0;
+  size_t counters_off = 0;
+  void* d_ws = nullptr;
+  int device = -1;
+};
+
+namespace nx {
+
+static int batch_item_mode(const nx_esrrf_item& it) {
+  return (it.n_sens > 0 || it.corr_mask == NX_CORR_AVG) ? kModeSum : kModeFull;
+}
+
+}  // namespace nx
+
+extern "C" {
+
+int nx_esrrf_batch_create(nx_esrrf_batch** out, const nx_esrrf_item* items, int n) {
+  if (!out) return invalid("batch out-pointer is NULL");
+  *out = nullptr;
+  if (n < 1 || !items) return invalid("empty batch");
+  int dev = -1;
+  NX_CUDA_TRY(cudaGetDevice(&dev));
+  auto* b = new nx_esrrf_batch();
+  b->device = dev;
+  const int sms = device_sms();
+  for (int i = 0; i < n; ++i) {
+    const nx_esrrf_item& it = items[i];
+    const nx_esrrf_plan* p = it.plan;
+    int rc = check_plan(p);
+    if (rc) { delete b; return rc; }
+    if (!p->fused) {
+      delete b;
+      set_error("batch item %d: magnification %d / radius %g has no fused kernel", i, p->M,
+                (double)p->radius);
+      return NX_ERR_UNSUPPORTED;
+    }
+    if (it.T < 1 || !it.d_in || !it.d_out) { delete b; return invalid("batch item without frames or buffers"); }
+    if (it.n_sens < 0 || it.n_sens > kMaxSens) { delete b; return invalid("n_sens must be 0..4"); }
+    if (it.corr_mask <= 0 || it.corr_mask > 7) { delete b; return invalid("Type of correlation must be AVG, VAR or TAC2"); }
+    if (it.n_sens > 0 && it.corr_mask != NX_CORR_AVG) { delete b; return invalid("sensitivity sweeps are AVG only"); }
+    nx_esrrf_batch::Item bi;
+    bi.desc = it;
+    bi.mode = batch_item_mode(it);
+    bi.n_out = it.n_sens > 0 ? it.n_sens : corr_count(it.corr_mask);
+    bi.fpt = (it.frames_per_timepoint <= 0 || it.frames_per_timepoint > it.T) ? it.T
+                                                                                : it.frames_per_timepoint;
+    bi.n_tp = (it.T + bi.fpt - 1) / bi.fpt;
+    const int min_nf = std::min(bi.fpt, it.T - (bi.n_tp - 1) * bi.fpt);
+    int fpu = it.frames_per_unit;
+    if (fpu <= 0) {
+      // heuristic: enough units for ~3 waves of this item alone, >= 8 frames each
+      const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + p->fused->geo.TY - 1) / p->fused->geo.TY);
+      long long c = (3LL * sms + tiles * bi.n_tp - 1) / (tiles * bi.n_tp);
+      c = std::min<long long>(c, std::max(1, min_nf / 8));
+      fpu = (int)std::max<long long>(1, (min_nf + c - 1) / c);
+    }
+    bi.chunks = std::max(1, std::min(min_nf, (min_nf + fpu - 1) / fpu));
+    bi.cls = -1;
+    // class by (kernel entry, mode)
+    for (size_t c = 0; c < b->classes.size(); ++c)
+      if (b->classes[c].entry == p->fused && b->classes[c].mode == bi.mode) bi.cls = (int)c;
+    if (bi.cls < 0) {
+      nx_esrrf_batch::Class cl;
+      cl.entry = p->fused;
+      cl.mode = bi.mode;
+      cl.grid = 0;
+      memset(&cl.maps, 0, sizeof(cl.maps));
+      b->classes.push_back(cl);
+      bi.cls = (int)b->classes.size() - 1;
+    }
+    b->classes[bi.cls].items.push_back(i);
+    b->items.push_back(bi);
+  }
+  // workspace layout
+  size_t off = kStatusBytes;
+  b->counters_off = off;
+  off += align256(b->classes.size() * sizeof(unsigned));
+  for (auto& cl : b->classes) {
+    cl.params_off = off;
+    off += align256(cl.items.size() * sizeof(FusedParams));
+    cl.starts_off = off;
+    off += align256((cl.items.size() + 1) * sizeof(int));
+    cl.unit_start.assign(1, 0);
+    for (int idx : cl.items) {
+      const auto& bi = b->items[idx];
+      const nx_esrrf_plan* p = bi.desc.plan;
+      const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + p->fused->geo.TY - 1) / p->fused->geo.TY);
+      const long long u = (long long)cl.unit_start.back() + tiles * bi.n_tp * bi.chunks;
+      if (u > 0x7fffffffLL) { delete b; return invalid("batch too large for one launch"); }
+      cl.unit_start.push_back((int)u);
+    }
+    cl.ns_cap = 1;
+    for (int idx : cl.items) cl.ns_cap = std::max(cl.ns_cap, b->items[idx].desc.n_sens);
+    const int occ = cl.entry->occupancy[cl.mode](cl.ns_cap);
+    if (occ < 1) {
+      delete b;
+      set_error("a batch class needs more shared memory than a CTA can hold "
+                "(too many sensitivities at this magnification)");
+      return NX_ERR_UNSUPPORTED;
+    }
+    cl.grid = std::min(cl.unit_start.back(), occ * sms);
+  }
+  for (auto& bi : b->items) {
+    const nx_esrrf_plan* p = bi.desc.plan;
+    const size_t planeM = (size_t)p->rowsM * p->colsM;
+    const int F = bi.mode == kModeFull ? 5 : 2 * bi.n_out;
+    bi.rec_off = off;
+    off += align256((size_t)bi.n_tp * bi.chunks * F * planeM * sizeof(float));
+    bi.mpc_off = off;
+    off += nx_macro_pixel_workspace_bytes(bi.n_out * bi.n_tp, p->M);
+  }
+  b->ws_bytes = off;
+  *out = b;
+  return NX_OK;
+}
+
+size_t nx_esrrf_batch_workspace_bytes(const nx_esrrf_batch* b) { return b ? b->ws_bytes : 0; }
+
+int nx_esrrf_batch_bind(nx_esrrf_batch* b, void* d_ws, size_t ws_bytes, void* stream) {
+  if (!b) return invalid("batch is NULL");
+  if (!d_ws || ws_bytes < b->ws_bytes) {
+    set_error("workspace too small: need %zu bytes", b->ws_bytes);
+    return NX_ERR_WORKSPACE;
+  }
+  int dev = -1;
+  NX_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != b->device) return invalid("batch bound on another device than it was created on");
+  cudaStream_t s = (cudaStream_t)stream;
+  char* base = (char*)d_ws;
+  unsigned* status = (unsigned*)base;
+  for (size_t c = 0; c < b->classes.size(); ++c) {
+    auto& cl = b->classes[c];
+    std::vector<FusedParams> params(cl.items.size());
+    int nmaps = 0;
+    for (size_t k = 0; k < cl.items.size(); ++k) {
+      auto& bi = b->items[cl.items[k]];
+      const nx_esrrf_plan* p = bi.desc.plan;
+      FusedParams& fp = params[k];
+      fill_params(p, fp, bi.desc.d_in, bi.desc.T, bi.fpt, bi.n_tp, bi.chunks,
+                  (float*)(base + bi.rec_off), status);
+      if (bi.mode == kModeSum) {
+        const int ns = bi.desc.n_sens > 0 ? bi.desc.n_sens : 1;
+        fp.n_sens = ns;
+        fp.F = 2 * ns;
+        for (int k2 = 0; k2 < ns && bi.desc.n_sens > 0; ++k2) {
+          const RgcScalars sc = rgc_scalars(p->M, p->radius, bi.desc.sens[k2], 0);
+          fp.sens_mode_k[k2] = sc.sens_mode;
+          fp.sens_int_k[k2] = sc.sens_int;
+          fp.sens_k[k2] = sc.sens;
+        }
+      } else {
+        fp.F = 5;
+      }
+      if (nmaps < kMaxTmaps && !tma_disabled() &&
+          make_frame_tmap(&cl.maps.m[nmaps], bi.desc.d_in, bi.desc.T, p->H, p->W,
+                          p->fused->geo.BW, p->fused->geo.BH))
+        fp.tmap = nmaps++;
+      bi.fp = fp;
+    }
+    NX_CUDA_TRY(cudaMemcpyAsync(base + cl.params_off, params.data(),
+                                params.size() * sizeof(FusedParams), cudaMemcpyHostToDevice, s));
+    NX_CUDA_TRY(cudaMemcpyAsync(base + cl.starts_off, cl.unit_start.data(),
+                                cl.unit_start.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+  }
+  NX_CUDA_TRY(cudaStreamSynchronize(s));
+  b->d_ws = d_ws;
+  return NX_OK;
+}
+
+int nx_esrrf_batch_launch(const nx_esrrf_batch* b, void* stream) {
+  if (!b || !b->d_ws) return invalid("batch is not bound to a workspace");
+  cudaStream_t s = (cudaStream_t)stream;
+  char* base = (char*)b->d_ws;
+  NX_CUDA_TRY(cudaMemsetAsync(base, 0, kStatusBytes + align256(b->classes.size() * sizeof(unsigned)),
+                              s));
+  for (size_t c = 0; c < b->classes.size(); ++c) {
+    const auto& cl = b->classes[c];
+    UnitTable ut;
+    memset(&ut, 0, sizeof(ut));
+    ut.items = (const FusedParams*)(base + cl.params_off);
+    ut.unit_start = (const int*)(base + cl.starts_off);
+    ut.n_items = (int)cl.items.size();
+    ut.total_units = cl.unit_start.back();
+    ut.counter = (unsigned*)(base + b->counters_off) + c;
+    ut.ns_cap = cl.ns_cap;
+    cudaError_t e = cl.entry->launch[cl.mode](ut, cl.maps, cl.grid, s);
+    if (e != cudaSuccess) return cuda_status(e, "batched eSRRF launch");
+  }
+  for (const auto& bi : b->items) {
+    const nx_esrrf_plan* p = bi.desc.plan;
+    const long long planeM = (long long)p->rowsM * p->colsM;
+    const bool full = bi.mode == kModeFull;
+    const int F = full ? 5 : 2 * bi.n_out;
+    const float* rec = (const float*)(base + bi.rec_off);
+    for (int tp = 0; tp < bi.n_tp; ++tp) {
+      const int nf = std::min(bi.fpt, bi.desc.T - tp * bi.fpt);
+      const int nch = std::min(bi.chunks, nf);
+      const float* rtp = rec + (size_t)tp * bi.chunks * F * planeM;
+      float* out = bi.desc.d_out + (size_t)tp * planeM;
+      const long long stride = (long long)bi.n_tp * planeM;
+      cudaError_t e;
+      if (full) {
+        e = launch_finalize(rtp, F, nch, nf, planeM, bi.desc.corr_mask, out, stride, true, s);
+      } else {
+        e = cudaSuccess;
+        for (int k = 0; k < bi.n_out && e == cudaSuccess; ++k)
+          e = launch_finalize(rtp + (size_t)2 * k * planeM, F, nch, nf, planeM, NX_CORR_AVG,
+                              out + (size_t)k * stride, stride, false, s);
+      }
+      if (e != cudaSuccess) return cuda_status(e, "batched temporal finalize");
+    }
+    if (bi.desc.macro_pixel_correction) {
+      cudaError_t e = launch_mpc(bi.desc.d_out, bi.n_out * bi.n_tp, p->rowsM, p->colsM, p->M,
+                                 (float*)(base + bi.mpc_off), s);
+      if (e != cudaSuccess) return cuda_status(e, "batched macro-pixel correction");
+    }
+  }
+  return NX_OK;
+}
+
+int nx_esrrf_batch_destroy(nx_esrrf_batch* b) {
+  delete b;
   return NX_OK;
 }
 

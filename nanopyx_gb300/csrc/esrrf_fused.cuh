@@ -22,6 +22,8 @@
 
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace nx {
@@ -31,6 +33,9 @@ enum FusedMode : int { kModeStack = 0, kModeSum = 1, kModeFull = 2 };
 __host__ __device__ constexpr int mode_fields(int mode) {
   return mode == kModeFull ? 5 : (mode == kModeSum ? 2 : 0);
 }
+
+constexpr int kMaxSens = 4;    // sensitivities sharing one RGC pass (AVG mode)
+constexpr int kMaxTmaps = 24;  // TMA descriptors carried in the kernel parameters
 
 struct FusedParams {
   const float* in;     // (T, H, W)
@@ -42,9 +47,6 @@ struct FusedParams {
   int chunks;          // chunks per timepoint (the last timepoint uses min(chunks, its frames))
   int margin;
   int iw;
-  int sens_mode;       // 0: none, 1: integer power sens_int, 2: powf(sens)
-  int sens_int;
-  float sens;
   int cy_base, cx_base;  // first tap row/col of the clamped half-grid index 2H / 2W
   float cy[4], cx[4];
   const float* tbl;      // [M][2J+1][3][NS4*4]  (a = dx*w/d, b = dy*w/d, w) per sample
@@ -52,13 +54,38 @@ struct FusedParams {
   const float* wfull;    // [M][M][2J+1][2J+1]
   float* out;            // stack (T, rowsM, colsM) or records [n_tp*chunks][F][rowsM][colsM]
   unsigned* status;
-  int use_tma;
+  int tmap;              // index into the kernel's TMA descriptor pack, or -1: plain loads
+  int tiles_y;
+  int F;                 // record fields: 5 (VAR/TAC2) or 2 * n_sens (AVG)
+  int n_sens;            // AVG mode: sensitivities evaluated on the same RGC (others: 1)
+  int sens_mode_k[kMaxSens];  // 0: none (s <= 1), 1: integer power sens_int_k, 2: powf(sens_k)
+  int sens_int_k[kMaxSens];
+  float sens_k[kMaxSens];
+};
+
+struct TmapPack {
+  CUtensorMap m[kMaxTmaps];
+};
+
+// Work list of one launch: units = (item, tile, timepoint, frame chunk), tiles
+// fastest.  One item may be carried by value (`single`); several live in
+// device memory with their first unit index in `unit_start`.  With `counter`
+// CTAs take units dynamically (persistent launch), else unit = blockIdx.x.
+struct UnitTable {
+  const FusedParams* items;
+  const int* unit_start;  // [n_items + 1]
+  int n_items;
+  int total_units;
+  unsigned* counter;
+  int ns_cap;  // largest n_sens among the items (sizes the AVG-mode temporal state)
+  FusedParams single;
 };
 
 template <int M>
 struct TileRows {
-  // input-pixel rows per CTA tile: keeps 32*TY*M threads <= 640
-  static constexpr int TY = (M <= 2) ? 8 : (M <= 4 ? 4 : 2);
+  // input-pixel rows per CTA tile (32*TY*M threads <= 640); measured: TY = 4 beats
+  // TY = 2 at m = 5 by 4 % despite one CTA per SM (less halo work per pixel)
+  static constexpr int TY = (M <= 2) ? 8 : (M <= 5 ? 4 : 2);
 };
 
 template <int M, int J, int TY>
@@ -86,7 +113,7 @@ struct Geo {
   static constexpr int RIW = TX + 4;
   static constexpr int NT = 32 * TY * M;
 
-  static constexpr int al(int n) { return (n + 31) / 32 * 32; }
+  __host__ __device__ static constexpr int al(int n) { return (n + 31) / 32 * 32; }
   // shared-memory layout (in floats, 128-byte aligned blocks)
   static constexpr int O_INB = 0;
   static constexpr int S_INB = al(BH * BW);
@@ -108,22 +135,39 @@ struct Geo {
   static constexpr int S_CW = al(OX * 5);
   // per-thread constants / state kept out of registers: [px][thread]
   static constexpr int O_TW = O_CW + S_CW;   // 1 / sum w per output
-  static constexpr int O_TK = O_TW + M * NT; // temporal shift K per output
-  static constexpr int O_BAR = O_TK + M * NT;
-  static constexpr int FLOATS = O_BAR + 32;
-  static constexpr size_t SMEM_BYTES = size_t(FLOATS) * 4;
+  static constexpr int O_TK = O_TW + M * NT; // temporal state: K (FULL) or K, S per sensitivity (SUM)
+  static constexpr int S_TK_FULL = 5 * M * NT;
+  static constexpr int O_BAR_FULL = O_TK + S_TK_FULL;
+  // AVG mode keeps K and S of ns_cap sensitivities per output
+  __host__ __device__ static constexpr int o_bar(int mode, int ns_cap) {
+    return mode == 1 ? O_TK + 2 * ns_cap * M * NT : (mode == 2 ? O_BAR_FULL : O_TK);
+  }
+  __host__ __device__ static constexpr size_t smem_bytes(int mode, int ns_cap) {
+    return size_t(o_bar(mode, ns_cap) + 32 + 64) * 4;
+  }
 };
 
 __device__ __forceinline__ float f4c(const float4& v, int e) {
   return e == 0 ? v.x : (e == 1 ? v.y : (e == 2 ? v.z : v.w));
 }
 
+__device__ __forceinline__ float apply_sens(float r, int mode, int n, float s) {
+  if (mode == 1) {
+    const float base = r;
+    for (int k = 1; k < n; ++k) r *= base;
+  } else if (mode == 2) {
+    r = powf(r, s);
+  }
+  return r;
+}
+
 template <int M, int J, int TY, int MODE>
 __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
-    esrrf_fused_kernel(const __grid_constant__ CUtensorMap tmap, const FusedParams p) {
+    esrrf_fused_kernel(const __grid_constant__ TmapPack maps, const UnitTable ut) {
   using G = Geo<M, J, TY>;
-  constexpr int F = mode_fields(MODE);
   extern __shared__ __align__(128) float sm[];
+  __shared__ FusedParams sp;
+  __shared__ int s_unit;
   float* inb = sm + G::O_INB;
   float* gsm = sm + G::O_G;
   float* t1 = sm + G::O_T1;
@@ -133,9 +177,10 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   float4* tb4 = reinterpret_cast<float4*>(sm + G::O_TB);
   float* rw = sm + G::O_RW;
   float* cw = sm + G::O_CW;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + G::O_BAR);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + G::o_bar(MODE, ut.ns_cap));
   float* tw = sm + G::O_TW;  // tw[px * NT + tid]
-  float* tk = sm + G::O_TK;  // tk[px * NT + tid]
+  float* tk = sm + G::O_TK;  // FULL: field f (K, S, Q, P, L) at tk[(f * M + px) * NT + tid];
+                             // SUM: K, S of sensitivity k at fields 2k, 2k + 1
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -143,20 +188,59 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   const int ty = warp % TY;
   const int py = warp / TY;
 
-  const int tile = blockIdx.x;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  unsigned ph0 = 0, ph1 = 0;  // completed phases of bar[0] / bar[1] (same in every thread)
+  int cur_item = -1;
+
+  for (int iter = 0;; ++iter) {
+  int unit;
+  if (ut.counter) {
+    if (tid == 0) s_unit = (int)atomicAdd(ut.counter, 1u);
+    __syncthreads();
+    unit = s_unit;
+  } else {
+    unit = blockIdx.x + iter * gridDim.x;
+  }
+  if (unit >= ut.total_units) break;
+  int item = 0;
+  if (ut.items) {
+    int lo = 0, hi = ut.n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(ut.unit_start + mid) <= unit) lo = mid;
+      else hi = mid - 1;
+    }
+    item = lo;
+  }
+  if (item != cur_item) {
+    if (tid == 0) sp = ut.items ? ut.items[item] : ut.single;
+    __syncthreads();
+    const float4* src = reinterpret_cast<const float4*>(sp.tbl);
+    for (int i = tid; i < M * G::W2 * 3 * G::NS4; i += G::NT) tb4[i] = src[i];
+    cur_item = item;
+  }
+  const FusedParams& p = sp;
+  const int local = unit - (ut.items ? __ldg(ut.unit_start + item) : 0);
+  const int tiles = p.tiles_x * p.tiles_y;
+  const int tile = local % tiles;
+  const int tp = (local / tiles) / p.chunks;
+  const int chunk = (local / tiles) % p.chunks;
   const int tile_x = tile % p.tiles_x;
   const int tile_y = tile / p.tiles_x;
   const int nx0 = tile_x * G::TX;
   const int ny0 = tile_y * TY;
-  const int tp = blockIdx.y / p.chunks;
-  const int chunk = blockIdx.y % p.chunks;
   const int H = p.H, W = p.W;
 
-  // frames of this CTA
+  // frames of this unit
   const int tp_f0 = tp * p.fpt;
   const int tp_nf = min(p.fpt, p.T - tp_f0);
   const int nch = min(p.chunks, tp_nf);
-  if (chunk >= nch) return;  // uniform across the CTA
+  if (chunk < nch) {  // uniform across the CTA
   const int f0 = tp_f0 + (int)((long long)chunk * tp_nf / nch);
   const int f1 = tp_f0 + (int)((long long)(chunk + 1) * tp_nf / nch);
 
@@ -171,8 +255,6 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
 
   // ---- per-CTA constants: RGC tables, intensity weights ------------------
   {
-    const float4* src = reinterpret_cast<const float4*>(p.tbl);
-    for (int i = tid; i < M * G::W2 * 3 * G::NS4; i += G::NT) tb4[i] = src[i];
     for (int i = tid; i < G::OY; i += G::NT) {
       const int yM = ny0 * M + i;
       const int ny = ny0 + i / M;
@@ -248,27 +330,16 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     }
   }
 
-  float accS[M], accQ[M], accP[M], accL[M];
-#pragma unroll
-  for (int px = 0; px < M; ++px) {
-    accS[px] = 0.f; accQ[px] = 0.f; accP[px] = 0.f; accL[px] = 0.f;
-  }
 
   constexpr unsigned kTileBytes = unsigned(G::BH * G::BW * 4);
-  const bool use_tma = p.use_tma != 0;
-  if (use_tma) {
-    if (tid == 0) {
-      mbar_init(&bar[0], 1);
-      mbar_init(&bar[1], 1);
-      fence_mbar_init();
-    }
-  }
+  const bool use_tma = p.tmap >= 0;
+  const CUtensorMap* tmap = use_tma ? &maps.m[p.tmap] : nullptr;
   __syncthreads();
   if (use_tma && tid == 0) {
     for (int k = 0; k < 2; ++k) {
       if (f0 + k < f1) {
         mbar_arrive_expect_tx(&bar[k], kTileBytes);
-        tma_load_3d(inb + k * G::S_INB, &tmap, &bar[k], x_start, y_start, f0 + k);
+        tma_load_3d(inb + k * G::S_INB, tmap, &bar[k], x_start, y_start, f0 + k);
       }
     }
   }
@@ -281,12 +352,14 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     const int b = it & 1;
     float* tin = inb + b * G::S_INB;
     if (use_tma) {
-      const bool ok = mbar_wait_bounded(&bar[b], (unsigned)((it >> 1) & 1));
+      const bool ok = mbar_wait_bounded(&bar[b], (b ? ph1 : ph0) & 1u);
       if (__syncthreads_or(!ok)) {
         if (tid == 0) atomicOr(p.status, kDevTmaTimeout);
         abort_it = it;
         break;
       }
+      if (b) ++ph1;
+      else ++ph0;
     } else {
       const float* src = p.in + (size_t)f * H * W;
       for (int i = tid; i < G::BH * G::BW; i += G::NT) {
@@ -329,7 +402,7 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     if (use_tma && tid == 0 && f + 2 < f1) {
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&bar[b], kTileBytes);
-      tma_load_3d(tin, &tmap, &bar[b], x_start, y_start, f + 2);
+      tma_load_3d(tin, tmap, &bar[b], x_start, y_start, f + 2);
     }
 
     // ---- phase 2: gradient column pass onto half-grid columns; intensity --
@@ -460,26 +533,45 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     const float* irow = inten + (ty * M + py) * G::OX + lane * M;
 #pragma unroll
     for (int px = 0; px < M; ++px) {
-      float r = acc[px] * tw[px * G::NT + tid];
-      r = (r < 0.f) ? 0.f : r;
-      if (p.sens_mode == 1) {
-        const float base = r;
-        for (int k = 1; k < p.sens_int; ++k) r *= base;
-      } else if (p.sens_mode == 2) {
-        r = powf(r, p.sens);
-      }
-      if (p.iw) r *= irow[px];
-      if (omask & (1u << px)) r = 0.f;
-      if (MODE == kModeStack) {
-        if (!(omask >> 31)) p.out[(size_t)f * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
+      float base = acc[px] * tw[px * G::NT + tid];
+      base = (base < 0.f) ? 0.f : base;
+      const float ival = p.iw ? irow[px] : 1.f;
+      const bool zero = (omask & (1u << px)) != 0;
+      if (MODE == kModeSum) {
+        for (int k = 0; k < p.n_sens; ++k) {
+          float r = apply_sens(base, p.sens_mode_k[k], p.sens_int_k[k], p.sens_k[k]);
+          r = zero ? 0.f : r * ival;
+          float* K = tk + ((2 * k) * M + px) * G::NT + tid;
+          float* S = tk + ((2 * k + 1) * M + px) * G::NT + tid;
+          if (it == 0) {
+            *K = r;
+            *S = 0.f;
+          } else {
+            *S += r - *K;
+          }
+        }
       } else {
-        if (it == 0) tk[px * G::NT + tid] = r;
-        const float y = r - tk[px * G::NT + tid];
-        accS[px] += y;
-        if (MODE == kModeFull) {
-          accQ[px] = fmaf(y, y, accQ[px]);
-          accP[px] = fmaf(accL[px], y, accP[px]);
-          accL[px] = y;
+        float r = apply_sens(base, p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
+        r = zero ? 0.f : r * ival;
+        if (MODE == kModeStack) {
+          if (!(omask >> 31))
+            p.out[(size_t)f * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
+        } else {
+          float* st = tk + px * G::NT + tid;
+          constexpr int FS = M * G::NT;  // field stride
+          if (it == 0) {
+            st[0] = r;
+            st[FS] = 0.f;
+            st[2 * FS] = 0.f;
+            st[3 * FS] = 0.f;
+            st[4 * FS] = 0.f;
+          } else {
+            const float y = r - st[0];
+            st[FS] += y;
+            st[2 * FS] = fmaf(y, y, st[2 * FS]);
+            st[3 * FS] = fmaf(st[4 * FS], y, st[3 * FS]);
+            st[4 * FS] = y;
+          }
         }
       }
     }
@@ -490,51 +582,89 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     // (this frame's and the next one's), then leave without writing
     if (tid == 0) {
       const int bb = abort_it & 1;
-      (void)mbar_wait_bounded(&bar[bb], (unsigned)((abort_it >> 1) & 1));
+      (void)mbar_wait_bounded(&bar[bb], (bb ? ph1 : ph0) & 1u);
       if (f0 + abort_it + 1 < f1)
-        (void)mbar_wait_bounded(&bar[bb ^ 1], (unsigned)(((abort_it + 1) >> 1) & 1));
+        (void)mbar_wait_bounded(&bar[bb ^ 1], (bb ? ph0 : ph1) & 1u);
     }
     return;
   }
 
   if (MODE != kModeStack && !(omask >> 31)) {
-    float* rec = p.out + (size_t)(tp * p.chunks + chunk) * F * plane + (size_t)yM * p.colsM +
-                 (size_t)nx * M;
+    float* rec = p.out + (size_t)(tp * p.chunks + chunk) * p.F * plane +
+                 (size_t)yM * p.colsM + (size_t)nx * M;
+    if (MODE == kModeSum) {
+      for (int k = 0; k < p.n_sens; ++k) {
 #pragma unroll
-    for (int px = 0; px < M; ++px) {
-      rec[px] = tk[px * G::NT + tid];
-      rec[plane + px] = accS[px];
-      if (MODE == kModeFull) {
-        rec[2 * plane + px] = accQ[px];
-        rec[3 * plane + px] = accP[px];
-        rec[4 * plane + px] = accL[px];
+        for (int px = 0; px < M; ++px) {
+          rec[(2 * k) * plane + px] = tk[((2 * k) * M + px) * G::NT + tid];
+          rec[(2 * k + 1) * plane + px] = tk[((2 * k + 1) * M + px) * G::NT + tid];
+        }
       }
+    } else {
+#pragma unroll
+      for (int fld = 0; fld < 5; ++fld)
+#pragma unroll
+        for (int px = 0; px < M; ++px)
+          rec[fld * plane + px] = tk[(fld * M + px) * G::NT + tid];
     }
   }
+  }  // chunk < nch
+  __syncthreads();  // the unit's shared state is free for the next unit
+  }  // unit loop
+}
+
+constexpr size_t kMaxSmemPerBlock = 227 * 1024;
+
+template <int M, int J, int MODE>
+size_t fused_smem_bytes(int ns_cap) {
+  constexpr int TY = TileRows<M>::TY;
+  return Geo<M, J, TY>::smem_bytes(MODE, ns_cap);
 }
 
 template <int M, int J, int MODE>
-cudaError_t launch_fused(const FusedParams& p, const CUtensorMap& tmap, cudaStream_t stream) {
+cudaError_t launch_fused(const UnitTable& ut, const TmapPack& maps, int grid,
+                         cudaStream_t stream) {
   constexpr int TY = TileRows<M>::TY;
   using G = Geo<M, J, TY>;
   auto kern = esrrf_fused_kernel<M, J, TY, MODE>;
-  static int attr_done = -1;  // device the attribute was last set for
+  const size_t smem = G::smem_bytes(MODE, MODE == kModeSum ? ut.ns_cap : 1);
+  if (smem + sizeof(FusedParams) + 64 > kMaxSmemPerBlock) return cudaErrorInvalidValue;
+  static int attr_done = -1;  // device the attributes were last set for
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (attr_done != dev) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)G::SMEM_BYTES);
+    const size_t cap = std::min(kMaxSmemPerBlock - sizeof(FusedParams) - 64,
+                                G::smem_bytes(MODE, MODE == kModeSum ? kMaxSens : 1));
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     attr_done = dev;
   }
-  const int tiles_y = (p.H + TY - 1) / TY;
-  dim3 grid((unsigned)(p.tiles_x * tiles_y), (unsigned)(p.n_tp * p.chunks));
-  kern<<<grid, G::NT, G::SMEM_BYTES, stream>>>(tmap, p);
+  if (grid < 1) return cudaSuccess;
+  kern<<<grid, G::NT, smem, stream>>>(maps, ut);
   return cudaGetLastError();
+}
+
+// resident CTAs per SM of one instantiation (for persistent grids)
+template <int M, int J, int MODE>
+int fused_occupancy(int ns_cap) {
+  constexpr int TY = TileRows<M>::TY;
+  using G = Geo<M, J, TY>;
+  const size_t smem = G::smem_bytes(MODE, MODE == kModeSum ? ns_cap : 1);
+  if (smem + sizeof(FusedParams) + 64 > kMaxSmemPerBlock) return 0;
+  int n = 0;
+  const size_t cap = std::min(kMaxSmemPerBlock - sizeof(FusedParams) - 64,
+                              G::smem_bytes(MODE, MODE == kModeSum ? kMaxSens : 1));
+  if (cudaFuncSetAttribute(esrrf_fused_kernel<M, J, TY, MODE>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap) != cudaSuccess)
+    return 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, esrrf_fused_kernel<M, J, TY, MODE>, G::NT,
+                                                    smem) != cudaSuccess)
+    return 1;
+  return n > 0 ? n : 1;
 }
 
 // geometry the host needs to build the tensor map for a given (M, J)

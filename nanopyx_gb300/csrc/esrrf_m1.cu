@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m1() {
   return FusedEntry{{&launch_fused<1, J, kModeStack>, &launch_fused<1, J, kModeSum>,
                      &launch_fused<1, J, kModeFull>},
+                    {&fused_occupancy<1, J, kModeStack>, &fused_occupancy<1, J, kModeSum>,
+                     &fused_occupancy<1, J, kModeFull>},
+                    {&fused_smem_bytes<1, J, kModeStack>, &fused_smem_bytes<1, J, kModeSum>,
+                     &fused_smem_bytes<1, J, kModeFull>},
                     fused_geometry<1, J>()};
 }
 

@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m2() {
   return FusedEntry{{&launch_fused<2, J, kModeStack>, &launch_fused<2, J, kModeSum>,
                      &launch_fused<2, J, kModeFull>},
+                    {&fused_occupancy<2, J, kModeStack>, &fused_occupancy<2, J, kModeSum>,
+                     &fused_occupancy<2, J, kModeFull>},
+                    {&fused_smem_bytes<2, J, kModeStack>, &fused_smem_bytes<2, J, kModeSum>,
+                     &fused_smem_bytes<2, J, kModeFull>},
                     fused_geometry<2, J>()};
 }
 

@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m3() {
   return FusedEntry{{&launch_fused<3, J, kModeStack>, &launch_fused<3, J, kModeSum>,
                      &launch_fused<3, J, kModeFull>},
+                    {&fused_occupancy<3, J, kModeStack>, &fused_occupancy<3, J, kModeSum>,
+                     &fused_occupancy<3, J, kModeFull>},
+                    {&fused_smem_bytes<3, J, kModeStack>, &fused_smem_bytes<3, J, kModeSum>,
+                     &fused_smem_bytes<3, J, kModeFull>},
                     fused_geometry<3, J>()};
 }
 

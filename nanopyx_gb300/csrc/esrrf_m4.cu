@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m4() {
   return FusedEntry{{&launch_fused<4, J, kModeStack>, &launch_fused<4, J, kModeSum>,
                      &launch_fused<4, J, kModeFull>},
+                    {&fused_occupancy<4, J, kModeStack>, &fused_occupancy<4, J, kModeSum>,
+                     &fused_occupancy<4, J, kModeFull>},
+                    {&fused_smem_bytes<4, J, kModeStack>, &fused_smem_bytes<4, J, kModeSum>,
+                     &fused_smem_bytes<4, J, kModeFull>},
                     fused_geometry<4, J>()};
 }
 

@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m5() {
   return FusedEntry{{&launch_fused<5, J, kModeStack>, &launch_fused<5, J, kModeSum>,
                      &launch_fused<5, J, kModeFull>},
+                    {&fused_occupancy<5, J, kModeStack>, &fused_occupancy<5, J, kModeSum>,
+                     &fused_occupancy<5, J, kModeFull>},
+                    {&fused_smem_bytes<5, J, kModeStack>, &fused_smem_bytes<5, J, kModeSum>,
+                     &fused_smem_bytes<5, J, kModeFull>},
                     fused_geometry<5, J>()};
 }
 

@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m6() {
   return FusedEntry{{&launch_fused<6, J, kModeStack>, &launch_fused<6, J, kModeSum>,
                      &launch_fused<6, J, kModeFull>},
+                    {&fused_occupancy<6, J, kModeStack>, &fused_occupancy<6, J, kModeSum>,
+                     &fused_occupancy<6, J, kModeFull>},
+                    {&fused_smem_bytes<6, J, kModeStack>, &fused_smem_bytes<6, J, kModeSum>,
+                     &fused_smem_bytes<6, J, kModeFull>},
                     fused_geometry<6, J>()};
 }
 

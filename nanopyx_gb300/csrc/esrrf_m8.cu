@@ -7,6 +7,10 @@ template <int J>
 static FusedEntry entry_m8() {
   return FusedEntry{{&launch_fused<8, J, kModeStack>, &launch_fused<8, J, kModeSum>,
                      &launch_fused<8, J, kModeFull>},
+                    {&fused_occupancy<8, J, kModeStack>, &fused_occupancy<8, J, kModeSum>,
+                     &fused_occupancy<8, J, kModeFull>},
+                    {&fused_smem_bytes<8, J, kModeStack>, &fused_smem_bytes<8, J, kModeSum>,
+                     &fused_smem_bytes<8, J, kModeFull>},
                     fused_geometry<8, J>()};
 }
 

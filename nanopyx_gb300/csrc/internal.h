@@ -13,9 +13,13 @@ namespace nx {
 // ---------------------------------------------------------------------------
 // fused eSRRF instantiations: one table entry per (M, J)
 // ---------------------------------------------------------------------------
-using FusedLaunchFn = cudaError_t (*)(const FusedParams&, const CUtensorMap&, cudaStream_t);
+using FusedLaunchFn = cudaError_t (*)(const UnitTable&, const TmapPack&, int, cudaStream_t);
+using FusedOccupancyFn = int (*)(int ns_cap);
+using FusedSmemFn = size_t (*)(int ns_cap);
 struct FusedEntry {
-  FusedLaunchFn launch[3];  // indexed by FusedMode
+  FusedLaunchFn launch[3];       // indexed by FusedMode
+  FusedOccupancyFn occupancy[3]; // resident CTAs per SM (0: does not fit)
+  FusedSmemFn smem[3];           // dynamic shared memory bytes
   FusedGeometry geo;
 };
 const FusedEntry* fused_entry(int M, int J);  // nullptr if not instantiated
@@ -67,7 +71,8 @@ cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n
 // combine `nchunks` consecutive records (each F planes) of one timepoint with frame
 // counts derived from nf, and write the correlations of corr_mask to out[ci*out_stride]
 cudaError_t launch_finalize(const float* rec, int F, int nchunks, int nf, long long n,
-                            int corr_mask, float* out, long long out_stride, cudaStream_t s);
+                            int corr_mask, float* out, long long out_stride, bool full,
+                            cudaStream_t s);
 cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int corr, float* out,
                                   cudaStream_t s);
 cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int order, float* out,

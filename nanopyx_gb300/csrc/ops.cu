@@ -297,8 +297,7 @@ __global__ void record_merge_kernel(float* __restrict__ acc, const float* __rest
 
 __global__ void finalize_kernel(const float* __restrict__ rec, int F, int nchunks, int nf,
                                 long long n, int corr_mask, float* __restrict__ out,
-                                long long out_stride) {
-  const bool full = F >= 5;
+                                long long out_stride, bool full) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     Rec a{0.f, 0.f, 0.f, 0.f, 0.f};
@@ -588,10 +587,11 @@ cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n
 }
 
 cudaError_t launch_finalize(const float* rec, int F, int nchunks, int nf, long long n,
-                            int corr_mask, float* out, long long out_stride, cudaStream_t s) {
+                            int corr_mask, float* out, long long out_stride, bool full,
+                            cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   finalize_kernel<<<grid_for(n), kBlock, 0, s>>>(rec, F, nchunks, nf, n, corr_mask, out,
-                                                 out_stride);
+                                                 out_stride, full);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,277 @@
+"""Batched eSRRF: uneven stacks and parameter sweeps in persistent launches.
+
+``EsrrfBatch`` plans many independent reconstructions -- different H, W, T,
+magnification, radius, sensitivity and correlation -- and runs them as one
+persistent kernel launch per kernel class (magnification, window half-width),
+every CTA taking (stack, tile, timepoint, frame-chunk) units from a shared
+work list, followed by the temporal finalisation and macro-pixel correction
+of every item.  The launch sequence can be captured into a CUDA graph once and
+replayed (``graph=True``).
+
+A sensitivity sweep at one radius is a single item with up to four
+sensitivities: the RGC map is evaluated once per frame and raised to each
+sensitivity in the epilogue, so a 4 x 4 (radius x sensitivity) grid costs four
+RGC passes instead of the sixteen full eSRRF runs of the reference sweep
+(``src/nanopyx/core/analysis/parameter_sweep.py:33-37``).
+
+``tune_frames_per_unit`` is the autotuner: it times the batch at several work
+unit sizes (frames per unit) and caches the fastest per GPU and kernel class
+in ``~/.cache/nanopyx_gb300/autotune.json``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import threading
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._device import check_image, get_plan, require_cuda, workspace
+
+__all__ = ["EsrrfBatch", "esrrf_batch", "sweep_batch", "tune_frames_per_unit"]
+
+_CACHE_PATH = os.path.join(os.path.expanduser("~"), ".cache", "nanopyx_gb300", "autotune.json")
+_cache_lock = threading.Lock()
+
+
+def _corr_mask(corr):
+    names = [corr] if isinstance(corr, str) else list(corr)
+    if not names or any(n not in N.CORR_BITS for n in names):
+        raise ValueError("Type of correlation must be AVG, VAR or TAC2")
+    m = 0
+    for n in names:
+        m |= N.CORR_BITS[n]
+    return names, m
+
+
+class EsrrfBatch:
+    """A fixed set of eSRRF reconstructions run as persistent batched launches.
+
+    ``add(stack, ...)`` registers one reconstruction (a (T, H, W) float32 CUDA
+    tensor or NumPy array, copied to the device once) and returns its index;
+    ``run()`` executes everything and returns the list of outputs, each
+    (n_outputs, n_timepoints, H*m, W*m) on the device (outputs follow the
+    requested correlation order, or the sensitivity order for a sweep item).
+    """
+
+    def __init__(self, device=None):
+        self.device = device if device is not None else require_cuda()
+        self._specs = []
+        self._handle = None
+        self._ws = None
+        self._graph = None
+        self.outputs = []
+
+    def add(self, stack, magnification: int = 5, radius: float = 1.5, sensitivity=1,
+            frames_per_timepoint: int = 0, temporal_correlation="AVG",
+            doIntensityWeighting: bool = True, macro_pixel_correction: bool = True,
+            frames_per_unit: int = 0) -> int:
+        if self._handle is not None:
+            raise RuntimeError("batch already planned")
+        if isinstance(stack, torch.Tensor):
+            t = check_image(stack).to(self.device).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(check_image(stack))).to(self.device)
+        T, H, W = t.shape
+        sens_list = list(sensitivity) if isinstance(sensitivity, (list, tuple)) else None
+        if sens_list is not None:
+            if not 1 <= len(sens_list) <= 4:
+                raise ValueError("a sweep item takes 1 to 4 sensitivities")
+            names, mask = _corr_mask("AVG")
+            if temporal_correlation != "AVG":
+                raise ValueError("sensitivity sweeps are AVG only")
+            plan_s = sens_list[0]
+        else:
+            names, mask = _corr_mask(temporal_correlation)
+            plan_s = sensitivity
+        m = int(magnification)
+        fpt = T if frames_per_timepoint == 0 or frames_per_timepoint > T else int(frames_per_timepoint)
+        n_tp = T // fpt + (1 if T % fpt else 0)
+        order = [b for b in ("AVG", "VAR", "TAC2") if mask & N.CORR_BITS[b]]
+        n_out = len(sens_list) if sens_list is not None else len(order)
+        out = torch.empty((n_out, n_tp, H * m, W * m), dtype=torch.float32, device=self.device)
+        plan = get_plan(H, W, m, radius, plan_s, doIntensityWeighting)
+        self._specs.append(dict(stack=t, plan=plan, T=T, fpt=fpt, mask=mask, names=names,
+                                order=order, sens=sens_list, mpc=bool(macro_pixel_correction),
+                                out=out, fpu=int(frames_per_unit), key=(m, float(radius))))
+        return len(self._specs) - 1
+
+    # -- planning -----------------------------------------------------------
+    def _items(self):
+        arr = (N.EsrrfItem * len(self._specs))()
+        for it, sp in zip(arr, self._specs):
+            it.plan = sp["plan"].handle
+            it.d_in = sp["stack"].data_ptr()
+            it.T = sp["T"]
+            it.frames_per_timepoint = sp["fpt"]
+            it.corr_mask = sp["mask"]
+            it.macro_pixel_correction = 1 if sp["mpc"] else 0
+            sens = sp["sens"] or []
+            it.n_sens = len(sens)
+            for k, v in enumerate(sens):
+                it.sens[k] = float(v)
+            it.frames_per_unit = sp["fpu"] or _cached_fpu(sp["key"])
+            it.d_out = sp["out"].data_ptr()
+        return arr
+
+    def plan(self):
+        if not self._specs:
+            raise ValueError("empty batch")
+        L = N.lib()
+        items = self._items()
+        h = C.c_void_p()
+        N.check(L.nx_esrrf_batch_create(C.byref(h), C.cast(items, C.c_void_p), len(self._specs)),
+                "eSRRF batch")
+        self._handle = h
+        self._ws = workspace(L.nx_esrrf_batch_workspace_bytes(h), self.device)
+        N.check(L.nx_esrrf_batch_bind(h, self._ws.data_ptr(), self._ws.numel(),
+                                      torch.cuda.current_stream(self.device).cuda_stream),
+                "eSRRF batch")
+        self.outputs = [sp["out"] for sp in self._specs]
+        return self
+
+    def launch(self, stream=None):
+        """Issue the batch on ``stream`` (default: current); capturable."""
+        if self._handle is None:
+            self.plan()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device).cuda_stream
+        N.check(N.lib().nx_esrrf_batch_launch(self._handle, s), "eSRRF batch")
+
+    def capture(self):
+        """Capture the launch sequence into a CUDA graph (after one eager run)."""
+        if self._handle is None:
+            self.plan()
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.launch(side.cuda_stream)  # warm-up: kernel attributes, lazy loading
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch(torch.cuda.current_stream(self.device).cuda_stream)
+        self._graph = g
+        return self
+
+    def run(self, graph: bool = False, check: bool = True):
+        if graph:
+            if self._graph is None:
+                self.capture()
+            self._graph.replay()
+        else:
+            self.launch()
+        if check:
+            N.check(N.lib().nx_workspace_status(
+                self._ws.data_ptr(), torch.cuda.current_stream(self.device).cuda_stream),
+                "eSRRF batch")
+        outs = []
+        for sp in self._specs:
+            o = sp["out"]
+            if sp["sens"] is None:
+                o = o[[sp["order"].index(n) for n in sp["names"]]]
+            outs.append(o)
+        return outs
+
+    def __del__(self):
+        try:
+            if self._handle is not None:
+                N.lib().nx_esrrf_batch_destroy(self._handle)
+        except Exception:
+            pass
+
+
+def esrrf_batch(stacks, params, graph: bool = False):
+    """Run ``eSRRF`` on every stack with its own keyword arguments in one batch.
+
+    ``params`` is a list of dicts with the keyword arguments of ``EsrrfBatch.add``.
+    Returns the list of device outputs (see ``EsrrfBatch``).
+    """
+    b = EsrrfBatch()
+    for st, kw in zip(stacks, params):
+        b.add(st, **kw)
+    return b.run(graph=graph)
+
+
+def sweep_batch(stack, magnification: int, sensitivities, radii, frames_per_timepoint: int = 0,
+                doIntensityWeighting: bool = True, macro_pixel_correction: bool = False,
+                graph: bool = False):
+    """The (sensitivity x radius) AVG reconstruction grid in one batch.
+
+    Returns a device tensor (len(sensitivities), len(radii), n_tp, H*m, W*m).
+    """
+    b = EsrrfBatch()
+    t = stack if isinstance(stack, torch.Tensor) else torch.from_numpy(
+        np.ascontiguousarray(check_image(stack)))
+    t = check_image(t).to(b.device).contiguous()
+    sens = list(sensitivities)
+    groups = [sens[i:i + 4] for i in range(0, len(sens), 4)]
+    index = {}
+    for r in radii:
+        for g in groups:
+            index[(float(r), tuple(g))] = b.add(t, magnification, r, list(g),
+                                                frames_per_timepoint, "AVG",
+                                                doIntensityWeighting, macro_pixel_correction)
+    outs = b.run(graph=graph)
+    rows = []
+    for si, s in enumerate(sens):
+        g = groups[si // 4]
+        k = si % 4
+        rows.append(torch.stack([outs[index[(float(r), tuple(g))]][k] for r in radii]))
+    return torch.stack(rows)
+
+
+# ---------------------------------------------------------------------------
+# autotuner: frames per work unit
+# ---------------------------------------------------------------------------
+def _gpu_key():
+    p = torch.cuda.get_device_properties(torch.cuda.current_device())
+    return f"{p.name}/{p.multi_processor_count}"
+
+
+def _load_cache():
+    try:
+        with open(_CACHE_PATH) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _cached_fpu(key) -> int:
+    m, r = key
+    J = int(np.float32(2.0) * np.float32(r))
+    return int(_load_cache().get(_gpu_key(), {}).get(f"m{m}_J{J}", 0))
+
+
+def tune_frames_per_unit(stack, magnification: int = 5, radius: float = 1.5,
+                         candidates=(8, 16, 32, 64, 0), repeats: int = 3,
+                         temporal_correlation="AVG", save: bool = True):
+    """Time one reconstruction at several frames-per-unit sizes; cache the best.
+
+    ``0`` means the built-in heuristic.  Returns (best, {candidate: ms}).
+    """
+    times = {}
+    for c in candidates:
+        b = EsrrfBatch()
+        b.add(stack, magnification, radius, 1, 0, temporal_correlation, frames_per_unit=c)
+        b.plan()
+        b.run(check=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(repeats):
+            b.run(check=False)
+        e1.record()
+        torch.cuda.synchronize()
+        times[c] = e0.elapsed_time(e1) / repeats
+    best = min(times, key=times.get)
+    if save:
+        J = int(np.float32(2.0) * np.float32(radius))
+        with _cache_lock:
+            data = _load_cache()
+            data.setdefault(_gpu_key(), {})[f"m{int(magnification)}_J{J}"] = int(best)
+            os.makedirs(os.path.dirname(_CACHE_PATH), exist_ok=True)
+            with open(_CACHE_PATH, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+    return best, times

@@ -228,30 +228,27 @@ class Workflow:
 
 def esrrf_parameter_sweep(img, magnification: int = 2, sensitivities=(1, 2), radii=(1, 1.5),
                           temporal_correlation: str = "AVG", frames_per_timepoint: int = 0,
-                          doIntensityWeighting: bool = True, macro_pixel_correction: bool = False):
+                          doIntensityWeighting: bool = True, macro_pixel_correction: bool = False,
+                          graph: bool = False):
     """Reconstruction grid of the eSRRF parameter sweep.
 
     Returns an array (len(sensitivities), len(radii), n_timepoints, H*m, W*m)
-    (squeezed over timepoints like ``eSRRF``).  The input is uploaded once and
-    each (sensitivity, radius) pair runs as one fused pass; the reference runs
-    a full, independent eSRRF_ST per pair (parameter_sweep.py:35-37).
-    For the single-launch batched form see ``nanopyx_gb300.engine``.
+    (squeezed over timepoints when there is one).  The whole grid runs as one
+    batch (``nanopyx_gb300.engine.sweep_batch``): one RGC pass per radius serves
+    up to four sensitivities; the reference runs a full, independent eSRRF_ST
+    per (sensitivity, radius) pair (parameter_sweep.py:35-37).
     """
-    st = to_device_stack(img)
-    outs = []
-    for s in sensitivities:
-        row = []
-        for r in radii:
-            o = esrrf_device(st.t, magnification, r, s, frames_per_timepoint,
-                             [temporal_correlation], doIntensityWeighting,
-                             macro_pixel_correction)[0]
-            row.append(o)
-        outs.append(torch.stack(row))
-    res = torch.stack(outs)
-    res = st.out(res)
-    if st.from_numpy and res.shape[2] == 1:
+    if temporal_correlation != "AVG":
+        raise ValueError("the batched sweep computes AVG reconstructions")
+    from .engine import sweep_batch
+
+    from_numpy = not (isinstance(img, torch.Tensor) and img.is_cuda)
+    res = sweep_batch(img if isinstance(img, torch.Tensor) else np.asarray(img), magnification,
+                      sensitivities, radii, frames_per_timepoint, doIntensityWeighting,
+                      macro_pixel_correction, graph=graph)
+    if res.shape[2] == 1:
         res = res[:, :, 0]
-    return res
+    return res.cpu().numpy() if from_numpy else res
 
 
 def run_esrrf_parameter_sweep(*args, **kwargs):
