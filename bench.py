@@ -383,12 +383,190 @@ def run_gpu_arm(args):
                                     "and packed f32x2 FFMA2 (no FP32 figure in MEASURED_PEAKS.json)"},
         "clocks": clocks,
     }
+    if not args.no_extras and args.workload == "large" and world == 1:
+        del x, out, ws
+        torch.cuda.empty_cache()
+        line["batched"] = bench_uneven_batch(dev)
+        torch.cuda.empty_cache()
+        line["sweep"] = bench_sweep(dev)
+        torch.cuda.empty_cache()
+        line["served"] = bench_served(dev)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = time_cpu_baseline(stack_np)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------------------
+# batched, sweep and served workloads (reported beside the headline line)
+# ---------------------------------------------------------------------------
+def _base_stacks(sizes, frames=25, density=0.006, seed=11):
+    from nanopyx_gb300.synthetic import blinking_stack, emitters_for_density
+
+    return {H: blinking_stack(frames, H, H, emitters_for_density(H, H, density), seed=seed + H)
+            for H in sizes}
+
+
+def _tile_frames(base, T):
+    reps = -(-T // base.shape[0])
+    return np.ascontiguousarray(np.concatenate([base] * reps)[:T])
+
+
+def bench_uneven_batch(dev, n_stacks=64, seed=3, repeats=2):
+    """64 stacks, H=W in {64,128,256,512}, T in [50,500], m in {2,4,5}, AVG/VAR/TAC2."""
+    import torch
+
+    import nanopyx_gb300 as nx
+    from nanopyx_gb300 import engine
+
+    rng = np.random.default_rng(seed)
+    sizes = [64, 128, 256, 512]
+    bases = _base_stacks(sizes)
+    stacks, params, mpxf = [], [], 0.0
+    for _ in range(n_stacks):
+        H = int(rng.choice(sizes))
+        T = int(rng.integers(50, 501))
+        x = torch.from_numpy(_tile_frames(bases[H], T)).to(dev)
+        stacks.append(x)
+        params.append(dict(magnification=int(rng.choice([2, 4, 5])), radius=1.5, sensitivity=1,
+                           temporal_correlation=str(rng.choice(["AVG", "VAR", "TAC2"]))))
+        mpxf += T * H * H / 1e6
+    b = engine.EsrrfBatch(dev)
+    for x, kw in zip(stacks, params):
+        b.add(x, **kw)
+    b.run(graph=True)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(repeats):
+        b.run(graph=True, check=False)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    t_batch = e0.elapsed_time(e1) / repeats / 1e3
+    # plain per-stack GPU path: one eSRRF call per stack, in turn
+    for x, kw in zip(stacks[:2], params[:2]):
+        nx.esrrf_device(x, kw["magnification"], kw["radius"], kw["sensitivity"], 0,
+                        kw["temporal_correlation"], check_status=False)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for x, kw in zip(stacks, params):
+        nx.esrrf_device(x, kw["magnification"], kw["radius"], kw["sensitivity"], 0,
+                        kw["temporal_correlation"], check_status=False)
+        torch.cuda.synchronize(dev)
+    t_plain = time.perf_counter() - t0
+    return {"workload": f"{n_stacks} uneven stacks, H=W in {{64,128,256,512}}, T in [50,500], "
+                        "m in {2,4,5}, R=1.5, s=1, AVG/VAR/TAC2 (one persistent launch per "
+                        "kernel class, CUDA graph)",
+            "mpx_frames": mpxf, "batched_value": mpxf / t_batch, "plain_value": mpxf / t_plain,
+            "unit": "Mpx*frames/s", "batched_s": t_batch, "plain_s": t_plain,
+            "speedup": t_plain / t_batch}
+
+
+def bench_sweep(dev, repeats=2):
+    """200 x 256 x 256, m=4, R in {1,1.5,2,2.5} x s in {1,2,3,4}, AVG: 16 outputs."""
+    import torch
+
+    import nanopyx_gb300 as nx
+    from nanopyx_gb300 import engine
+    from nanopyx_gb300.synthetic import blinking_stack
+
+    x = torch.from_numpy(blinking_stack(200, 256, 256, 150, seed=2)).to(dev)
+    sens, radii = [1, 2, 3, 4], [1.0, 1.5, 2.0, 2.5]
+    engine.sweep_batch(x, 4, sens, radii)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        engine.sweep_batch(x, 4, sens, radii)
+    torch.cuda.synchronize(dev)
+    t_sweep = (time.perf_counter() - t0) / repeats
+    t0 = time.perf_counter()
+    for s in sens:
+        for r in radii:
+            nx.esrrf_device(x, 4, r, s, 0, "AVG", macro_pixel_correction=False, check_status=False)
+    torch.cuda.synchronize(dev)
+    t_plain = time.perf_counter() - t0
+    mpxf = 200 * 256 * 256 / 1e6
+    return {"workload": "sweep 200x256x256, m=4, R in {1,1.5,2,2.5} x s in {1,2,3,4}, AVG "
+                        "(16 outputs; one RGC pass per radius shared by 4 sensitivities)",
+            "sweep_s": t_sweep, "plain_16_calls_s": t_plain, "speedup": t_plain / t_sweep,
+            "value": mpxf / t_sweep, "unit": "input Mpx*frames/s for the whole grid"}
+
+
+def bench_served(dev, n_requests=32, rate=8.0, block_interval=0.01, seed=9):
+    """Poisson arrivals; H=W log-uniform 64..1024; 1-10 blocks of 100 frames; m in {2,4,5}."""
+    import threading
+
+    import torch
+
+    from nanopyx_gb300.serve import ESRRFServer, serve_plain
+
+    rng = np.random.default_rng(seed)
+    sizes = [64, 90, 128, 181, 256, 362, 512, 724, 1024]
+    bases = _base_stacks(sizes)
+    blocks100 = {H: _tile_frames(bases[H], 100) for H in sizes}
+    reqs, t = [], 0.0
+    for _ in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        H = int(sizes[rng.integers(0, len(sizes))])
+        reqs.append(dict(t=t, H=H, nb=int(rng.integers(1, 11)), m=int(rng.choice([2, 4, 5]))))
+    total = sum(r["nb"] * 100 * r["H"] ** 2 / 1e6 for r in reqs)
+    # warm-up: plans and kernels of every (m, window) used
+    for m in (2, 4, 5):
+        serve_plain([[blocks100[64][:10]]], [dict(magnification=m)])
+    torch.cuda.synchronize(dev)
+
+    def run_served():
+        srv = ESRRFServer(n_streams=8, max_active=16)
+        handles = [None] * len(reqs)
+        events = sorted((r["t"] + k * block_interval, i, k) for i, r in enumerate(reqs)
+                        for k in range(r["nb"]))
+        t0 = time.perf_counter()
+
+        def feeder():
+            for ta, i, k in events:
+                dt = t0 + ta - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                if handles[i] is None:
+                    r = reqs[i]
+                    handles[i] = srv.submit(r["H"], r["H"], r["nb"], magnification=r["m"])
+                srv.push(handles[i], blocks100[reqs[i]["H"]])
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        for h in handles:
+            h.result(timeout=600)
+        srv.close()
+        t_end = max(h.t_done for h in handles) - t0
+        lat = [h.latency for h in handles]
+        return t_end, lat
+
+    def run_plain():
+        t0 = time.perf_counter()
+        lat, done = [], 0.0
+        for r in sorted(reqs, key=lambda r: r["t"]):
+            last = r["t"] + (r["nb"] - 1) * block_interval
+            dt = t0 + last - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            serve_plain([[blocks100[r["H"]]] * r["nb"]], [dict(magnification=r["m"])])
+            done = time.perf_counter() - t0
+            lat.append(done - last)
+        return done, lat
+
+    t_srv, lat_srv = run_served()
+    t_pl, lat_pl = run_plain()
+    pct = lambda a, q: float(np.percentile(np.asarray(a) * 1e3, q))  # noqa: E731
+    return {"workload": f"{n_requests} requests, Poisson {rate:g}/s, H=W log-uniform 64..1024, "
+                        f"1-10 blocks of 100 frames every {block_interval * 1e3:g} ms, m in {{2,4,5}}, "
+                        "R=1.5, s=1, AVG+MPC; latency = last block arrival -> result on host",
+            "mpx_frames": total,
+            "served": {"value": total / t_srv, "p50_ms": pct(lat_srv, 50), "p99_ms": pct(lat_srv, 99)},
+            "plain": {"value": total / t_pl, "p50_ms": pct(lat_pl, 50), "p99_ms": pct(lat_pl, 99)},
+            "unit": "Mpx*frames/s", "throughput_ratio": t_pl / t_srv}
 
 
 def main():
@@ -398,6 +576,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the uneven-batch, sweep and served-stream measurements")
     ap.add_argument("--workload", default="large", choices=["large", "small"],
                     help="small: 160 frames, 80 per timepoint (for ncu captures)")
     args = ap.parse_args()
