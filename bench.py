@@ -267,6 +267,19 @@ def run_reference_arm(args):
     return 0
 
 
+def max_over_ranks(value_ms: float, device=None) -> float:
+    """Largest timing over all ranks (every rank gets it); no-op without a process group."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value_ms)
+    t = torch.tensor([float(value_ms)], dtype=torch.float64,
+                     device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu_arm(args):
     import torch
 
@@ -329,10 +342,7 @@ def run_gpu_arm(args):
     _native.check(L.nx_workspace_status(ws.data_ptr(), stream.cuda_stream), "timed steps")
     total_ms = t_start.elapsed_time(t_stop)
     kern_ms = sum(a.elapsed_time(b) for a, b in k_ev) / args.steps
-    if dist is not None:
-        tt = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(total_ms, dev)
     ms_per_step = total_ms / args.steps
     mpxf = _mpx_frames(T, H, W)
     value = world * mpxf / (ms_per_step / 1e3)
@@ -391,6 +401,8 @@ def run_gpu_arm(args):
         line["sweep"] = bench_sweep(dev)
         torch.cuda.empty_cache()
         line["served"] = bench_served(dev)
+        torch.cuda.empty_cache()
+        line["srrf"] = bench_srrf(dev, stack_np)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = time_cpu_baseline(stack_np)
     print(json.dumps(line), flush=True)
@@ -567,6 +579,44 @@ def bench_served(dev, n_requests=32, rate=8.0, block_interval=0.01, seed=9):
             "served": {"value": total / t_srv, "p50_ms": pct(lat_srv, 50), "p99_ms": pct(lat_srv, 99)},
             "plain": {"value": total / t_pl, "p50_ms": pct(lat_pl, 50), "p99_ms": pct(lat_pl, 99)},
             "unit": "Mpx*frames/s", "throughput_ratio": t_pl / t_srv}
+
+
+def bench_srrf(dev, stack_np, frames=20, repeats=2):
+    """SRRF (ring 0.5, 12 ring points, m=5) + order-1 temporal mean on the 512 x 512 stack."""
+    import torch
+
+    import nanopyx_gb300 as nx
+
+    x = torch.from_numpy(np.ascontiguousarray(stack_np[:frames])).to(dev)
+
+    def one():
+        rad = nx.SRRF(x, magnification=5, ringRadius=0.5)
+        return nx.calculate_SRRF_temporal_correlations(rad, 1)
+
+    one()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        one()
+    torch.cuda.synchronize(dev)
+    dt = (time.perf_counter() - t0) / repeats
+    res = {"workload": f"SRRF {frames}x512x512, m=5, ring 0.5 (12 points), MPC, order-1 mean",
+           "value": frames * 512 * 512 / 1e6 / dt, "unit": "Mpx*frames/s", "seconds": dt}
+    if cpu_reference_available():
+        from oracle import ref_build
+
+        R = ref_build.load()
+        smp = np.ascontiguousarray(stack_np[:2])
+        mag = R["CRShiftAndMagnify"](verbose=False).run(smp, 0, 0, 5, 5, run_type="Threaded")
+        t0 = time.perf_counter()
+        rad = R["Radiality"](verbose=False).run(smp, mag, magnification=5, ringRadius=0.5,
+                                                run_type="Threaded")
+        R["macro_pixel_corrector"](rad, magnification=5)
+        cdt = time.perf_counter() - t0
+        res["cpu_reference"] = {"value": 2 * 512 * 512 / 1e6 / cdt, "cores": os.cpu_count(),
+                                "sample": "2 frames, compiled reference Radiality(Threaded) + "
+                                          "macro_pixel_corrector (magnified input precomputed)"}
+    return res
 
 
 def main():

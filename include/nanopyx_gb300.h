@@ -183,6 +183,14 @@ int nx_radiality(const float* d_img, const float* d_img_interp, int T, int h, in
                  int do_intensity_weighting, float* d_out, void* d_ws, size_t ws_bytes,
                  void* stream);
 
+/* SRRF(): magnified intensity, radiality and per-frame macro-pixel
+ * correction in one call, d_img (T, h, w) -> d_out (T, h*m, w*m).
+ *   src/nanopyx/methods/srrf/SRRF_workflow.py:9-76                          */
+size_t nx_srrf_workspace_bytes(int T, int h, int w, int magnification);
+int nx_srrf(const float* d_img, int T, int h, int w, int magnification, float ring_radius,
+            int border, int positivity_constraint, int do_intensity_weighting,
+            int macro_pixel_correction, float* d_out, void* d_ws, size_t ws_bytes, void* stream);
+
 /* eSRRF temporal correlation of a stack (T, n_pixels) -> (n_pixels).
  *   src/nanopyx/core/transform/sr_temporal_correlations.py:46-75,205-221    */
 int nx_temporal_correlation(const float* d_stack, int T, long long n_pixels, int correlation,

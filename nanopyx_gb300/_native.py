@@ -82,6 +82,8 @@ _SIGS = {
     "nx_rgc": (_I, [_P, _P, _P, _I, _I, _I, _I, _FL, _FL, _I, _I, _P, _P]),
     "nx_radiality_workspace_bytes": (_SZ, [_I, _I, _I]),
     "nx_radiality": (_I, [_P, _P, _I, _I, _I, _I, _FL, _I, _I, _I, _P, _P, _SZ, _P]),
+    "nx_srrf_workspace_bytes": (_SZ, [_I, _I, _I, _I]),
+    "nx_srrf": (_I, [_P, _I, _I, _I, _I, _FL, _I, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_temporal_correlation": (_I, [_P, _I, _LL, _I, _P, _P]),
     "nx_srrf_temporal_correlation": (_I, [_P, _I, _LL, _I, _P, _P]),
     "nx_macro_pixel_workspace_bytes": (_SZ, [_I, _I]),

@@ -978,9 +978,15 @@ int nx_radiality(const float* d_img, const float* d_img_interp, int T, int h, in
     return NX_ERR_WORKSPACE;
   }
   cudaStream_t s = (cudaStream_t)stream;
+  const RingCoords rc = ring_coords(magnification, ring_radius);
+  cudaError_t e = launch_srrf_fused(d_img, d_img_interp, T, h, w, magnification, rc, ring_radius,
+                                    border, positivity ? 1 : 0, iw ? 1 : 0, d_out, s);
+  if (e == cudaSuccess) return NX_OK;
+  if (e != cudaErrorNotSupported) return cuda_status(e, "Radiality");
+  (void)cudaGetLastError();
   float* gx = (float*)d_ws;
   float* gy = gx + (size_t)T * h * w;
-  cudaError_t e = launch_gradient_radiality(d_img, T, h, w, gx, gy, s);
+  e = launch_gradient_radiality(d_img, T, h, w, gx, gy, s);
   if (e == cudaSuccess)
     e = launch_radiality(gx, gy, d_img_interp, T, h, w, magnification,
                          ring_coords(magnification, ring_radius), border, positivity ? 1 : 0,
@@ -1006,6 +1012,54 @@ int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n, int o
   cudaError_t e = launch_srrf_temporal(d_stack, T, n, order, d_out, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_status(e, "SRRF temporal correlation");
   return NX_OK;
+}
+
+int nx_srrf(const float* d_img, int T, int h, int w, int magnification, float ring_radius,
+            int border, int positivity, int iw, int mpc, float* d_out, void* d_ws,
+            size_t ws_bytes, void* stream) {
+  if (T < 0 || h < 1 || w < 1) return invalid("bad image shape");
+  if (magnification < 1) return invalid("magnification must be >= 1");
+  const size_t need = std::max(nx_radiality_workspace_bytes(T, h, w) +
+                                   align256((size_t)T * h * magnification * w * magnification * 4),
+                               nx_macro_pixel_workspace_bytes(T, magnification));
+  if (!d_ws || ws_bytes < need) {
+    set_error("workspace too small: need %zu bytes", need);
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const RingCoords rc = ring_coords(magnification, ring_radius);
+  cudaError_t e = launch_srrf_fused(d_img, nullptr, T, h, w, magnification, rc, ring_radius,
+                                    border, positivity ? 1 : 0, iw ? 1 : 0, d_out, s);
+  if (e == cudaErrorNotSupported) {
+    (void)cudaGetLastError();
+    // general path: magnified intensity, gradients and the per-pixel kernel
+    float* mag = (float*)((char*)d_ws + nx_radiality_workspace_bytes(T, h, w));
+    float* zeros = (float*)d_ws;  // shift arrays (T zeros) at the start of the workspace
+    e = cudaMemsetAsync(zeros, 0, (size_t)std::max(T, 1) * sizeof(float), s);
+    if (e == cudaSuccess)
+      e = launch_cr_shift_magnify(d_img, T, h, w, zeros, zeros, (float)magnification,
+                                  (float)magnification, h * magnification, w * magnification,
+                                  mag, s);
+    float* gx = (float*)d_ws;
+    float* gy = gx + (size_t)T * h * w;
+    if (e == cudaSuccess) e = launch_gradient_radiality(d_img, T, h, w, gx, gy, s);
+    if (e == cudaSuccess)
+      e = launch_radiality(gx, gy, mag, T, h, w, magnification, rc, border, positivity ? 1 : 0,
+                           iw ? 1 : 0, d_out, s);
+  }
+  if (e != cudaSuccess) return cuda_status(e, "SRRF");
+  if (mpc) {
+    e = launch_mpc(d_out, T, h * magnification, w * magnification, magnification, (float*)d_ws,
+                   s);
+    if (e != cudaSuccess) return cuda_status(e, "SRRF macro-pixel correction");
+  }
+  return NX_OK;
+}
+
+size_t nx_srrf_workspace_bytes(int T, int h, int w, int magnification) {
+  return std::max(nx_radiality_workspace_bytes(T, h, w) +
+                      align256((size_t)T * h * magnification * w * magnification * 4),
+                  nx_macro_pixel_workspace_bytes(T, magnification));
 }
 
 size_t nx_macro_pixel_workspace_bytes(int S, int magnification) {

@@ -62,6 +62,11 @@ RingCoords ring_coords(int M, float ring_radius);
 cudaError_t launch_radiality(const float* gx, const float* gy, const float* img_interp, int T,
                              int h, int w, int M, const RingCoords& rc, int border, int positivity,
                              int iw, float* out, cudaStream_t s);
+// fused tile kernel (srrf_fused.cu); img_interp may be nullptr (intensity computed
+// in the kernel); cudaErrorNotSupported when (M, ring radius) is not covered
+cudaError_t launch_srrf_fused(const float* in, const float* img_interp, int T, int h, int w,
+                              int M, const RingCoords& rc, float ring_radius, int border,
+                              int positivity, int iw, float* out, cudaStream_t s);
 
 // temporal records: fields K, S, Q, P, L (planes of n_pixels)
 cudaError_t launch_record_push_frame(const float* frame, long long n, float* rec, int it,

@@ -181,15 +181,23 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
 def SRRF(image, magnification: int = 5, ringRadius: float = 0.5, border: int = 0,
          radialityPositivityConstraint: bool = True, doIntensityWeighting: bool = True,
          macro_pixel_correction: bool = True, _force_run_type=None):
-    """SRRF per-frame radiality stack (T, H*m, W*m), macro-pixel corrected per frame."""
+    """SRRF per-frame radiality stack (T, H*m, W*m), macro-pixel corrected per frame.
+
+    One fused pass per frame block: the magnified intensity is formed inside the
+    radiality kernel instead of being materialised (the reference's two-step
+    CRShiftAndMagnify -> Radiality workflow, SRRF_workflow.py:50-67).
+    """
     st = to_device_stack(image)
-    mag = ShiftAndMagnify().run(st.t, 0, 0, magnification, magnification)
-    rad = Radiality().run(st.t, mag, magnification=magnification, ringRadius=ringRadius,
-                          border=border, radialityPositivityConstraint=radialityPositivityConstraint,
-                          doIntensityWeighting=doIntensityWeighting)
-    if macro_pixel_correction:
-        rad = macro_pixel_corrector(rad, magnification)
-    return st.out(rad)
+    T, h, w = st.shape
+    m = int(magnification)
+    L = N.lib()
+    out = torch.empty((T, h * m, w * m), dtype=torch.float32, device=st.t.device)
+    ws = workspace(L.nx_srrf_workspace_bytes(T, h, w, m), st.t.device)
+    N.check(L.nx_srrf(st.ptr(), T, h, w, m, float(ringRadius), int(border),
+                      1 if radialityPositivityConstraint else 0, 1 if doIntensityWeighting else 0,
+                      1 if macro_pixel_correction else 0, out.data_ptr(), ws.data_ptr(),
+                      ws.numel(), stream_ptr()), "SRRF")
+    return st.out(out)
 
 
 class Workflow:

@@ -196,3 +196,13 @@ def test_large_frame_properties():
     ref = O.esrrf_st(x[:1, :96, :96], 5, 1.5, 2)
     # interior of the crop only (the crop's own border differs from the full frame's)
     assert rel_err(st[0, 40:400, 40:400], ref[0, 40:400, 40:400]) <= TOL
+
+
+@pytest.mark.parametrize("m,ring,border", [(5, 0.5, 0), (3, 1.5, 1), (7, 0.5, 0), (4, 2.5, 0)])
+def test_srrf_fused_and_general_paths_against_oracle(m, ring, border):
+    """m in {2,3,4,5,6,8} with ring <= 2 px run the fused kernel, the rest the general one."""
+    x = blinking_stack(2, 21, 26, 4, seed=m * 10 + border)
+    got = nx.SRRF(x, magnification=m, ringRadius=ring, border=border)
+    mag = O.cr_shift_magnify(x, 0, 0, m, m)
+    ref = O.macro_pixel_correct(O.radiality(x, mag, m, ring, border), m)
+    assert rel_err(got, ref) <= TOL
