@@ -626,6 +626,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--srrf-only", action="store_true",
+                    help="only the SRRF measurement (profiling the radiality kernel)")
+    ap.add_argument("--srrf-frames", type=int, default=20)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the uneven-batch, sweep and served-stream measurements")
     ap.add_argument("--workload", default="large", choices=["large", "small"],
@@ -635,6 +638,16 @@ def main():
         CFG.update(SMALL)
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.srrf_only:
+        import torch
+
+        from nanopyx_gb300.synthetic import blinking_stack
+
+        torch.cuda.set_device(0)
+        st = blinking_stack(args.srrf_frames, CFG["H"], CFG["W"], CFG["emitters"], seed=CFG["seed"])
+        print(json.dumps(bench_srrf(torch.device("cuda", 0), st, frames=args.srrf_frames)),
+              flush=True)
+        return 0
     return run_gpu_arm(args)
 
 

@@ -41,7 +41,8 @@ struct SrrfTile {
   static constexpr int O_RW = O_INT + al(OY * OX);      // intensity row weights [OY][5]
   static constexpr int O_CW = O_RW + al(OY * 5);        // intensity col weights [OX][5]
   static constexpr int O_RT = O_CW + al(OX * 5);        // ring row taps [OY][12][8]
-  static constexpr int O_CT = O_RT + al(OY * kRing * 8);  // ring col taps [OX][12][8]
+  // ring col taps: float4 halves [ring][px][2][lane] (lane-contiguous, conflict-free)
+  static constexpr int O_CT = O_RT + al(OY * kRing * 8);
   static constexpr int FLOATS = O_CT + al(OX * kRing * 8);
   static constexpr size_t SMEM = size_t(FLOATS) * 4;
 };
@@ -55,6 +56,7 @@ struct SrrfParams {
   int chunks;           // frame chunks (grid y)
   int border, positivity, iw;
   float rr;         // ring radius * M (float, as the reference)
+  float inv_rr;     // 1 / rr
   float xr[kRing], yr[kRing];
 };
 
@@ -135,7 +137,14 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
 #pragma unroll
     for (int k = 0; k < 5; ++k) cw[i * 5 + k] = w5[k];
     const float xc = (float)xM + 0.5f;
-    for (int s = 0; s < kRing; ++s) ring_entry(ct + (i * kRing + s) * 8, xc, p.xr[s], M, w);
+    const int ln = i / M, pxi = i % M;
+    for (int s = 0; s < kRing; ++s) {
+      float e[8];
+      ring_entry(e, xc, p.xr[s], M, w);
+      float4* dst = reinterpret_cast<float4*>(ct) + ((s * M + pxi) * 2) * 32 + ln;
+      dst[0] = make_float4(e[0], e[1], e[2], e[3]);
+      dst[32] = make_float4(e[4], e[5], e[6], e[7]);
+    }
   }
 
   const int ny = ny0 + ty, nx = nx0 + lane;
@@ -196,16 +205,15 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
       const int i = nx * M + px;  // output column
       float val = 0.f;
       if (row_ok && nx < w && i >= lo_i && i < hi_i) {
-        const float* crow = ct + ((lane * M + px) * kRing) * 8;
+        const float4* crow = reinterpret_cast<const float4*>(ct) + (px * 2) * 32 + lane;
         float div = 0.f;
 #pragma unroll 2
         for (int s = 0; s < kRing; ++s) {
           const float* re = rrow + s * 8;
-          const float* ce = crow + s * 8;
           const float4 rA = *reinterpret_cast<const float4*>(re);
           const float4 rB = *reinterpret_cast<const float4*>(re + 4);
-          const float4 cA = *reinterpret_cast<const float4*>(ce);
-          const float4 cB = *reinterpret_cast<const float4*>(ce + 4);
+          const float4 cA = crow[(s * M * 2) * 32];
+          const float4 cB = crow[(s * M * 2 + 1) * 32];
           float dk = 0.f;
           float vgx = 0.f, vgy = 0.f;
           if (rB.z != 0.f && cB.z != 0.f) {
@@ -226,10 +234,10 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
               vgx = fmaf(ax, wc[u], vgx);
               vgy = fmaf(ay, wc[u], vgy);
             }
-            const float gmag = sqrtf(vgx * vgx + vgy * vgy);
-            if (gmag != 0.f) {
+            const float g2 = vgx * vgx + vgy * vgy;
+            if (g2 != 0.f) {
               // |vGy (xc - x0) - vGx (yc - y0)| / GMag / ringRadius
-              dk = 1.f - (fabsf(vgy * cB.y - vgx * rB.y) / gmag) / p.rr;
+              dk = 1.f - fabsf(vgy * cB.y - vgx * rB.y) * rsqrtf(g2) * p.inv_rr;
               dk = dk * dk;
             }
           }
@@ -291,6 +299,7 @@ cudaError_t launch_srrf_fused(const float* in, const float* img_interp, int T, i
   p.positivity = positivity;
   p.iw = iw;
   p.rr = rc.radius;
+  p.inv_rr = rc.radius != 0.f ? 1.f / rc.radius : 0.f;
   for (int k = 0; k < kRing; ++k) {
     p.xr[k] = rc.x[k];
     p.yr[k] = rc.y[k];
