@@ -89,6 +89,15 @@ int nx_esrrf_run_stage2(const nx_esrrf_plan* plan, int T, int frames_per_timepoi
                         int corr_mask, int macro_pixel_correction, float* d_out, void* d_ws,
                         size_t ws_bytes, void* stream);
 
+/* Failure-detection self-test (not a reference routine): one CTA waits on an
+ * mbarrier that nothing arrives on, with the bounded wait every TMA wait of
+ * the fused kernels uses, limited to `limit_ns` (<= 1 s).  The kernel returns
+ * on its own and records the time-out in the status word of `d_ws`, so
+ * nx_workspace_status() then reports NX_ERR_DEVICE_TIMEOUT and the context
+ * stays usable.                                                              */
+int nx_selftest_wait_timeout(void* d_ws, size_t ws_bytes, unsigned long long limit_ns,
+                             void* stream);
+
 /* Throughput probe (not a reference routine): `blocks` CTAs of 256 threads
  * each run `iters` iterations of 8 independent FP32 FMA chains; returns via
  * d_sink (blocks*256 floats) so nothing is optimised away.  Used to measure

@@ -65,6 +65,7 @@ _SIGS = {
     "nx_esrrf_run": (_I, [_P, _P, _I, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_esrrf_run_stage1": (_I, [_P, _P, _I, _I, _I, _P, _SZ, _P]),
     "nx_esrrf_run_stage2": (_I, [_P, _I, _I, _I, _I, _P, _P, _SZ, _P]),
+    "nx_selftest_wait_timeout": (_I, [_P, _SZ, C.c_ulonglong, _P]),
     "nx_probe_ffma": (_I, [_P, _I, _I, _P]),
     "nx_probe_ffma2": (_I, [_P, _I, _I, _P]),
     "nx_esrrf_accum_bytes": (_SZ, [_P]),

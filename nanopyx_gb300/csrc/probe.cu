@@ -32,7 +32,35 @@ __global__ void __launch_bounds__(256) ffma2_probe_kernel(float* sink, int iters
       a0.x + a0.y + a1.x + a1.y + a2.x + a2.y + a3.x + a3.y;
 }
 
+// One CTA waits on an mbarrier that nothing arrives on, with the same bounded
+// wait the fused kernels use; on time-out it records the same status bit.
+__global__ void wait_timeout_selftest_kernel(unsigned* status, unsigned long long limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    nx::mbar_init(&bar, 1);
+    nx::fence_mbar_init();
+  }
+  __syncthreads();
+  const bool ok = nx::mbar_wait_bounded(&bar, 0u, limit_ns);
+  if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(status, nx::kDevTmaTimeout);
+  __syncthreads();
+  if (threadIdx.x == 0) nx::mbar_inval(&bar);
+}
+
 }  // namespace
+
+extern "C" int nx_selftest_wait_timeout(void* d_ws, size_t ws_bytes, unsigned long long limit_ns,
+                                        void* stream) {
+  if (!d_ws || ws_bytes < 256) return NX_ERR_WORKSPACE;
+  if (limit_ns > 1000000000ull) return NX_ERR_INVALID_ARG;  // keep the self-test short
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(d_ws, 0, sizeof(unsigned), s);
+  if (e == cudaSuccess) {
+    wait_timeout_selftest_kernel<<<1, 64, 0, s>>>((unsigned*)d_ws, limit_ns);
+    e = cudaGetLastError();
+  }
+  return e == cudaSuccess ? NX_OK : nx::cuda_status(e, "wait self-test");
+}
 
 extern "C" int nx_probe_ffma2(float* d_sink, int blocks, int iters, void* stream) {
   if (!d_sink || blocks < 1 || iters < 1) return NX_ERR_INVALID_ARG;
