@@ -373,7 +373,7 @@ int nx_esrrf_plan_create(nx_esrrf_plan** out, int H, int W, int magnification, f
   p->fused = (p->JW >= 1 && p->JW <= 6) ? fused_entry(magnification, p->JW) : nullptr;
   if (p->fused) {
     // instantiations whose shared-memory layout does not fit a CTA use the general path
-    const size_t lim = kMaxSmemPerBlock - sizeof(FusedParams) - 64;
+    const size_t lim = kSmemBudget;
     for (int mode = 0; mode < 3; ++mode)
       if (p->fused->smem[mode](1) > lim) p->fused = nullptr;
   }

@@ -88,7 +88,13 @@ struct TileRows {
   static constexpr int TY = (M <= 2) ? 8 : (M <= 5 ? 4 : 2);
 };
 
-template <int M, int J, int TY>
+// Frames per pass (FP).  With FP = 2 a thread carries two consecutive frames
+// through each pass of the frame loop: the RGC core runs on packed f32x2
+// arithmetic (frame pair in one register pair, one phase-table load for both
+// frames) and the preparation shares its index and weight work.  Results are
+// bit-identical to FP = 1 (the same IEEE operations per frame).
+// Instantiations whose FP = 2 shared-memory layout does not fit a CTA use FP = 1.
+template <int M, int J, int TY, int FP>
 struct Geo {
   static constexpr int TX = 32;
   static constexpr int W2 = 2 * J + 1;
@@ -112,30 +118,34 @@ struct Geo {
   static constexpr int OX = TX * M;
   static constexpr int RIW = TX + 4;
   static constexpr int NT = 32 * TY * M;
+  // phase-table block per (py, jj), in float4:
+  //   FP = 1: a[NS4] b[NS4] w[NS4]                    (4 samples per float4)
+  //   FP = 2: aa[2 NS4] bb[2 NS4] nb[2 NS4] w[NS4]    (a, b, -b duplicated into frame pairs)
+  static constexpr int TBLK = (FP == 2 ? 7 : 3) * NS4;
 
   __host__ __device__ static constexpr int al(int n) { return (n + 31) / 32 * 32; }
   // shared-memory layout (in floats, 128-byte aligned blocks)
   static constexpr int O_INB = 0;
-  static constexpr int S_INB = al(BH * BW);
-  static constexpr int O_G = O_INB + 2 * S_INB;
-  static constexpr int S_G = al(NRY * NCX);
-  static constexpr int O_T1 = O_G + 2 * S_G;
-  static constexpr int S_T1 = al(NRY * HG_C);
-  static constexpr int O_HG = O_T1 + 2 * S_T1;
-  static constexpr int S_HG = al(HG_R * 2 * HGP * 2);
+  static constexpr int S_INB = al(BH * BW);  // 2 * FP input tiles (two sets of FP frames)
+  static constexpr int O_G = O_INB + 2 * FP * S_INB;
+  static constexpr int S_G = al(NRY * NCX);  // Roberts-Cross gc, gr per frame
+  static constexpr int O_T1 = O_G + 2 * FP * S_G;
+  static constexpr int S_T1 = al(NRY * HG_C);  // column-pass gx, gy per frame
+  static constexpr int O_HG = O_T1 + 2 * FP * S_T1;
+  static constexpr int S_HG = al(HG_R * 2 * HGP * 2 * FP);  // unit gradients: float2 / float4
   static constexpr int O_RI = O_HG + S_HG;
-  static constexpr int S_RI = al(OY * RIW);
-  static constexpr int O_IN = O_RI + S_RI;
-  static constexpr int S_IN = al(OY * OX);
+  static constexpr int S_RI = al(OY * RIW);  // intensity row pass per frame
+  static constexpr int O_IN = O_RI + FP * S_RI;
+  static constexpr int S_IN = al(OY * OX * FP);  // magnified intensity: float / float2
   static constexpr int O_TB = O_IN + S_IN;
-  static constexpr int S_TB = al(M * W2 * 3 * NS4 * 4);
+  static constexpr int S_TB = al(M * W2 * TBLK * 4);
   static constexpr int O_RW = O_TB + S_TB;
   static constexpr int S_RW = al(OY * 5);
   static constexpr int O_CW = O_RW + S_RW;
   static constexpr int S_CW = al(OX * 5);
   // per-thread constants / state kept out of registers: [px][thread]
-  static constexpr int O_TW = O_CW + S_CW;   // 1 / sum w per output
-  static constexpr int O_TK = O_TW + M * NT; // temporal state: K (FULL) or K, S per sensitivity (SUM)
+  static constexpr int O_TW = O_CW + S_CW;    // 1 / sum w per output
+  static constexpr int O_TK = O_TW + M * NT;  // temporal state: K (FULL) or K, S per sensitivity (SUM)
   static constexpr int S_TK_FULL = 5 * M * NT;
   static constexpr int O_BAR_FULL = O_TK + S_TK_FULL;
   // AVG mode keeps K and S of ns_cap sensitivities per output
@@ -145,6 +155,18 @@ struct Geo {
   __host__ __device__ static constexpr size_t smem_bytes(int mode, int ns_cap) {
     return size_t(o_bar(mode, ns_cap) + 32 + 64) * 4;
   }
+};
+
+constexpr size_t kMaxSmemPerBlock = 227 * 1024;
+constexpr size_t kSmemBudget = kMaxSmemPerBlock - sizeof(FusedParams) - 64;
+
+// compile-time configuration of one instantiation
+template <int M, int J, int MODE>
+struct FusedCfg {
+  static constexpr int TY = TileRows<M>::TY;
+  static constexpr int NSC = MODE == kModeSum ? kMaxSens : 1;
+  static constexpr int FP = Geo<M, J, TY, 2>::smem_bytes(MODE, NSC) <= kSmemBudget ? 2 : 1;
+  using G = Geo<M, J, TY, FP>;
 };
 
 __device__ __forceinline__ float f4c(const float4& v, int e) {
@@ -161,18 +183,18 @@ __device__ __forceinline__ float apply_sens(float r, int mode, int n, float s) {
   return r;
 }
 
-template <int M, int J, int TY, int MODE>
+template <int M, int J, int TY, int FP, int MODE>
 __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     esrrf_fused_kernel(const __grid_constant__ TmapPack maps, const UnitTable ut) {
-  using G = Geo<M, J, TY>;
+  using G = Geo<M, J, TY, FP>;
   extern __shared__ __align__(128) float sm[];
   __shared__ FusedParams sp;
   __shared__ int s_unit;
   float* inb = sm + G::O_INB;
-  float* gsm = sm + G::O_G;
-  float* t1 = sm + G::O_T1;
-  float2* hg = reinterpret_cast<float2*>(sm + G::O_HG);
-  float* ri = sm + G::O_RI;
+  float* gsm = sm + G::O_G;   // plane 2 fr: gc, 2 fr + 1: gr
+  float* t1 = sm + G::O_T1;   // plane 2 fr: gx, 2 fr + 1: gy (half-grid columns)
+  float* hgf = sm + G::O_HG;  // FP = 1: float2 (nx, ny); FP = 2: float4 (nx0, nx1, ny0, ny1)
+  float* ri = sm + G::O_RI;   // plane fr
   float* inten = sm + G::O_IN;
   float4* tb4 = reinterpret_cast<float4*>(sm + G::O_TB);
   float* rw = sm + G::O_RW;
@@ -189,12 +211,12 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   const int py = warp / TY;
 
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int k = 0; k < 2 * FP; ++k) mbar_init(&bar[k], 1);
     fence_mbar_init();
   }
   __syncthreads();
-  unsigned ph0 = 0, ph1 = 0;  // completed phases of bar[0] / bar[1] (same in every thread)
+  unsigned phase = 0;  // bit k: parity of the next completion of bar[k] (same in every thread)
+  unsigned pend = 0;   // bit k: a TMA load into input buffer k is in flight
   int cur_item = -1;
 
   for (int iter = 0;; ++iter) {
@@ -220,8 +242,29 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   if (item != cur_item) {
     if (tid == 0) sp = ut.items ? ut.items[item] : ut.single;
     __syncthreads();
-    const float4* src = reinterpret_cast<const float4*>(sp.tbl);
-    for (int i = tid; i < M * G::W2 * 3 * G::NS4; i += G::NT) tb4[i] = src[i];
+    if constexpr (FP == 1) {
+      const float4* src = reinterpret_cast<const float4*>(sp.tbl);
+      for (int i = tid; i < M * G::W2 * 3 * G::NS4; i += G::NT) tb4[i] = src[i];
+    } else {
+      // plan layout [py][jj]{a, b, w}[NS4 * 4] -> frame-pair layout of Geo::TBLK
+      constexpr int N4 = G::NS4 * 4;
+      const float* src = sp.tbl;
+      float* dst = reinterpret_cast<float*>(tb4);
+      for (int i = tid; i < M * G::W2 * N4; i += G::NT) {
+        const int blk = i / N4, s = i % N4;
+        const float a = src[(blk * 3 + 0) * N4 + s];
+        const float b = src[(blk * 3 + 1) * N4 + s];
+        const float w = src[(blk * 3 + 2) * N4 + s];
+        float* d = dst + blk * G::TBLK * 4;
+        d[2 * s] = a;
+        d[2 * s + 1] = a;
+        d[2 * N4 + 2 * s] = b;
+        d[2 * N4 + 2 * s + 1] = b;
+        d[4 * N4 + 2 * s] = -b;
+        d[4 * N4 + 2 * s + 1] = -b;
+        d[6 * N4 + s] = w;
+      }
+    }
     cur_item = item;
   }
   const FusedParams& p = sp;
@@ -253,7 +296,7 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   const int twoH = 2 * H, twoW = 2 * W;
   const int kmax_y = 2 * p.rowsM - 2, kmax_x = 2 * p.colsM - 2;
 
-  // ---- per-CTA constants: RGC tables, intensity weights ------------------
+  // ---- per-CTA constants: intensity interpolation weights -----------------
   {
     for (int i = tid; i < G::OY; i += G::NT) {
       const int yM = ny0 * M + i;
@@ -330,42 +373,61 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     }
   }
 
-
   constexpr unsigned kTileBytes = unsigned(G::BH * G::BW * 4);
   const bool use_tma = p.tmap >= 0;
   const CUtensorMap* tmap = use_tma ? &maps.m[p.tmap] : nullptr;
   __syncthreads();
-  if (use_tma && tid == 0) {
-    for (int k = 0; k < 2; ++k) {
+  if (use_tma) {
+    // input buffer k = set * FP + fr holds frame f0 + k for the first two sets
+    if (tid == 0) fence_proxy_async_smem();
+    for (int k = 0; k < 2 * FP; ++k) {
       if (f0 + k < f1) {
-        mbar_arrive_expect_tx(&bar[k], kTileBytes);
-        tma_load_3d(inb + k * G::S_INB, tmap, &bar[k], x_start, y_start, f0 + k);
+        if (tid == 0) {
+          mbar_arrive_expect_tx(&bar[k], kTileBytes);
+          tma_load_3d(inb + k * G::S_INB, tmap, &bar[k], x_start, y_start, f0 + k);
+        }
+        pend |= 1u << k;
       }
     }
   }
 
   const size_t plane = (size_t)p.rowsM * p.colsM;
-  int abort_it = -1;
+  bool aborted = false;
 
-  for (int f = f0; f < f1; ++f) {
-    const int it = f - f0;
-    const int b = it & 1;
-    float* tin = inb + b * G::S_INB;
+  for (int fa = f0; fa < f1; fa += FP) {
+    const int set = ((fa - f0) / FP) & 1;
+    const int nf = min(FP, f1 - fa);  // frames of this pass (the last pass may hold one)
+    const float* tin[FP];
+#pragma unroll
+    for (int fr = 0; fr < FP; ++fr)
+      tin[fr] = inb + (set * FP + (fr < nf ? fr : 0)) * G::S_INB;
     if (use_tma) {
-      const bool ok = mbar_wait_bounded(&bar[b], (b ? ph1 : ph0) & 1u);
+      bool ok = true;
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        const int k = set * FP + fr;
+        if (fr < nf && ok) {
+          ok = mbar_wait_bounded(&bar[k], (phase >> k) & 1u);
+          if (ok) {
+            phase ^= 1u << k;
+            pend &= ~(1u << k);
+          }
+        }
+      }
       if (__syncthreads_or(!ok)) {
         if (tid == 0) atomicOr(p.status, kDevTmaTimeout);
-        abort_it = it;
+        aborted = true;
         break;
       }
-      if (b) ++ph1;
-      else ++ph0;
     } else {
-      const float* src = p.in + (size_t)f * H * W;
-      for (int i = tid; i < G::BH * G::BW; i += G::NT) {
-        const int r = y_start + i / G::BW;
-        const int c = x_start + i % G::BW;
-        tin[i] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(src + (size_t)r * W + c) : 0.f;
+      for (int fr = 0; fr < nf; ++fr) {
+        const float* src = p.in + (size_t)(fa + fr) * H * W;
+        float* dst = inb + (set * FP + fr) * G::S_INB;
+        for (int i = tid; i < G::BH * G::BW; i += G::NT) {
+          const int r = y_start + i / G::BW;
+          const int c = x_start + i % G::BW;
+          dst[i] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(src + (size_t)r * W + c) : 0.f;
+        }
       }
       __syncthreads();
     }
@@ -374,79 +436,123 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     for (int i = tid; i < G::NRY * G::NCX; i += G::NT) {
       const int rl = i / G::NCX, cl = i % G::NCX;
       const int r = RY0 + rl, c = CX0 + cl;
-      float gc = 0.f, gr = 0.f;
-      if (r >= 0 && r < H && c >= 0 && c < W) {
-        const int r0 = r > 0 ? r - 1 : 0;
-        const int c0 = c > 0 ? c - 1 : 0;
-        const float a = tin[(r0 - y_start) * G::BW + (c - x_start)];   // image[r0][c1]
-        const float bb = tin[(r - y_start) * G::BW + (c0 - x_start)];  // image[r1][c0]
-        const float d = tin[(r0 - y_start) * G::BW + (c0 - x_start)];  // image[r0][c0]
-        const float e = tin[(r - y_start) * G::BW + (c - x_start)];    // image[r1][c1]
-        gc = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
-        gr = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
+      const bool in = r >= 0 && r < H && c >= 0 && c < W;
+      const int r0 = r > 0 ? r - 1 : 0;
+      const int c0 = c > 0 ? c - 1 : 0;
+      const int ia = (r0 - y_start) * G::BW + (c - x_start);   // image[r0][c1]
+      const int ib = (r - y_start) * G::BW + (c0 - x_start);   // image[r1][c0]
+      const int id = (r0 - y_start) * G::BW + (c0 - x_start);  // image[r0][c0]
+      const int ie = (r - y_start) * G::BW + (c - x_start);    // image[r1][c1]
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        float gc = 0.f, gr = 0.f;
+        if (in) {
+          const float a = tin[fr][ia], bb = tin[fr][ib], d = tin[fr][id], e = tin[fr][ie];
+          gc = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
+          gr = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
+        }
+        gsm[(2 * fr) * G::S_G + i] = gc;
+        gsm[(2 * fr + 1) * G::S_G + i] = gr;
       }
-      gsm[i] = gc;
-      gsm[G::S_G + i] = gr;
     }
     for (int i = tid; i < G::OY * G::RIW; i += G::NT) {
       const int oy = i / G::RIW, cc = i % G::RIW;
       const int nyo = ny0 + oy / M;
-      const float* w5 = rw + oy * 5;
-      const float* col = tin + (nyo - 2 - y_start) * G::BW + (nx0 - 2 + cc - x_start);
-      float s = 0.f;
+      float w5[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) s = fmaf(w5[k], col[k * G::BW], s);
-      ri[i] = s;
+      for (int k = 0; k < 5; ++k) w5[k] = rw[oy * 5 + k];
+      const int off = (nyo - 2 - y_start) * G::BW + (nx0 - 2 + cc - x_start);
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        const float* col = tin[fr] + off;
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s = fmaf(w5[k], col[k * G::BW], s);
+        ri[fr * G::S_RI + i] = s;
+      }
     }
     __syncthreads();
-    if (use_tma && tid == 0 && f + 2 < f1) {
-      fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&bar[b], kTileBytes);
-      tma_load_3d(tin, tmap, &bar[b], x_start, y_start, f + 2);
+    if (use_tma) {
+      // this set's input buffers are free: fetch the frames two passes ahead
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        const int fn = fa + 2 * FP + fr;
+        const int k = set * FP + fr;
+        if (fn < f1) {
+          if (tid == 0) {
+            if (fr == 0) fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[k], kTileBytes);
+            tma_load_3d(inb + k * G::S_INB, tmap, &bar[k], x_start, y_start, fn);
+          }
+          pend |= 1u << k;
+        }
+      }
     }
 
     // ---- phase 2: gradient column pass onto half-grid columns; intensity --
     for (int i = tid; i < G::NRY * G::HG_C; i += G::NT) {
       const int rl = i / G::HG_C, kxl = i % G::HG_C;
       const int kx = kb_x + kxl;
-      float vc = 0.f, vr = 0.f;
+      float vc[FP], vr[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) vc[fr] = vr[fr] = 0.f;
       if (kx >= 1 && kx <= kmax_x) {
-        const float* g0 = gsm + rl * G::NCX;
-        const float* g1 = gsm + G::S_G + rl * G::NCX;
         if (kx >= twoW) {
 #pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const int cl = p.cx_base + t - CX0;
-            vc = fmaf(p.cx[t], g0[cl], vc);
-            vr = fmaf(p.cx[t], g1[cl], vr);
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX;
+            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int cl = p.cx_base + t - CX0;
+              vc[fr] = fmaf(p.cx[t], g0[cl], vc[fr]);
+              vr[fr] = fmaf(p.cx[t], g1[cl], vr[fr]);
+            }
           }
         } else if (kx & 1) {
           const int cl = ((kx - 1) >> 1) - CX0;
-          vc = g0[cl];
-          vr = g1[cl];
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            vc[fr] = gsm[(2 * fr) * G::S_G + rl * G::NCX + cl];
+            vr[fr] = gsm[(2 * fr + 1) * G::S_G + rl * G::NCX + cl];
+          }
         } else {
           const int cl = (kx >> 1) - 2 - CX0;
-          vc = -0.0625f * g0[cl];
-          vr = -0.0625f * g1[cl];
-          vc = fmaf(0.5625f, g0[cl + 1], vc);
-          vr = fmaf(0.5625f, g1[cl + 1], vr);
-          vc = fmaf(0.5625f, g0[cl + 2], vc);
-          vr = fmaf(0.5625f, g1[cl + 2], vr);
-          vc = fmaf(-0.0625f, g0[cl + 3], vc);
-          vr = fmaf(-0.0625f, g1[cl + 3], vr);
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX + cl;
+            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX + cl;
+            float c = -0.0625f * g0[0], r = -0.0625f * g1[0];
+            c = fmaf(0.5625f, g0[1], c);
+            r = fmaf(0.5625f, g1[1], r);
+            c = fmaf(0.5625f, g0[2], c);
+            r = fmaf(0.5625f, g1[2], r);
+            vc[fr] = fmaf(-0.0625f, g0[3], c);
+            vr[fr] = fmaf(-0.0625f, g1[3], r);
+          }
         }
       }
-      t1[i] = vc;
-      t1[G::S_T1 + i] = vr;
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        t1[(2 * fr) * G::S_T1 + i] = vc[fr];
+        t1[(2 * fr + 1) * G::S_T1 + i] = vr[fr];
+      }
     }
     for (int i = tid; i < G::OY * G::OX; i += G::NT) {
       const int oy = i / G::OX, ox = i % G::OX;
-      const float* w5 = cw + ox * 5;
-      const float* rr = ri + oy * G::RIW + ox / M;
-      float s = 0.f;
+      float w5[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) s = fmaf(w5[k], rr[k], s);
-      inten[i] = s;
+      for (int k = 0; k < 5; ++k) w5[k] = cw[ox * 5 + k];
+      const int ro = oy * G::RIW + ox / M;
+      float s[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        s[fr] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[fr] = fmaf(w5[k], ri[fr * G::S_RI + ro + k], s[fr]);
+      }
+      if constexpr (FP == 2) reinterpret_cast<float2*>(inten)[i] = make_float2(s[0], s[1]);
+      else inten[i] = s[0];
     }
     __syncthreads();
 
@@ -454,137 +560,244 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     for (int i = tid; i < G::HG_R * G::HG_C; i += G::NT) {
       const int kyl = i / G::HG_C, kxl = i % G::HG_C;
       const int ky = kb_y + kyl, kx = kb_x + kxl;
-      float2 n = make_float2(0.f, 0.f);
+      float nxv[FP], nyv[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) nxv[fr] = nyv[fr] = 0.f;
       if (ky >= 1 && ky <= kmax_y && kx >= 1 && kx <= kmax_x) {
-        const float* c0 = t1 + kxl;
-        const float* c1 = t1 + G::S_T1 + kxl;
-        float gx = 0.f, gy = 0.f;
+        float gx[FP], gy[FP];
         if (ky >= twoH) {
 #pragma unroll
-          for (int t = 0; t < 4; ++t) {
-            const int rl = p.cy_base + t - RY0;
-            gx = fmaf(p.cy[t], c0[rl * G::HG_C], gx);
-            gy = fmaf(p.cy[t], c1[rl * G::HG_C], gy);
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* c0 = t1 + (2 * fr) * G::S_T1 + kxl;
+            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + kxl;
+            gx[fr] = gy[fr] = 0.f;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int rl = p.cy_base + t - RY0;
+              gx[fr] = fmaf(p.cy[t], c0[rl * G::HG_C], gx[fr]);
+              gy[fr] = fmaf(p.cy[t], c1[rl * G::HG_C], gy[fr]);
+            }
           }
         } else if (ky & 1) {
           const int rl = ((ky - 1) >> 1) - RY0;
-          gx = c0[rl * G::HG_C];
-          gy = c1[rl * G::HG_C];
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            gx[fr] = t1[(2 * fr) * G::S_T1 + rl * G::HG_C + kxl];
+            gy[fr] = t1[(2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl];
+          }
         } else {
           const int rl = (ky >> 1) - 2 - RY0;
-          gx = -0.0625f * c0[rl * G::HG_C];
-          gy = -0.0625f * c1[rl * G::HG_C];
-          gx = fmaf(0.5625f, c0[(rl + 1) * G::HG_C], gx);
-          gy = fmaf(0.5625f, c1[(rl + 1) * G::HG_C], gy);
-          gx = fmaf(0.5625f, c0[(rl + 2) * G::HG_C], gx);
-          gy = fmaf(0.5625f, c1[(rl + 2) * G::HG_C], gy);
-          gx = fmaf(-0.0625f, c0[(rl + 3) * G::HG_C], gx);
-          gy = fmaf(-0.0625f, c1[(rl + 3) * G::HG_C], gy);
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* c0 = t1 + (2 * fr) * G::S_T1 + rl * G::HG_C + kxl;
+            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl;
+            float x = -0.0625f * c0[0], y = -0.0625f * c1[0];
+            x = fmaf(0.5625f, c0[G::HG_C], x);
+            y = fmaf(0.5625f, c1[G::HG_C], y);
+            x = fmaf(0.5625f, c0[2 * G::HG_C], x);
+            y = fmaf(0.5625f, c1[2 * G::HG_C], y);
+            gx[fr] = fmaf(-0.0625f, c0[3 * G::HG_C], x);
+            gy[fr] = fmaf(-0.0625f, c1[3 * G::HG_C], y);
+          }
         }
-        const float m2 = fmaf(gx, gx, gy * gy);
-        if (m2 > 0.f) {
-          const float inv = rsqrtf(m2);
-          n = make_float2(gx * inv, gy * inv);
+#pragma unroll
+        for (int fr = 0; fr < FP; ++fr) {
+          const float m2 = fmaf(gx[fr], gx[fr], gy[fr] * gy[fr]);
+          if (m2 > 0.f) {
+            const float inv = rsqrtf(m2);
+            nxv[fr] = gx[fr] * inv;
+            nyv[fr] = gy[fr] * inv;
+          }
         }
       }
-      hg[(kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1)] = n;
+      const int o = (kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1);
+      if constexpr (FP == 2)
+        reinterpret_cast<float4*>(hgf)[o] = make_float4(nxv[0], nxv[1], nyv[0], nyv[1]);
+      else
+        reinterpret_cast<float2*>(hgf)[o] = make_float2(nxv[0], nyv[0]);
     }
     __syncthreads();
 
     // ---- phase 4: RGC for this thread's M outputs --------------------------
     // contribution of sample (phase, offset): (dp < 0) ? w - |u| : 0 with
     // dp = n.(a, b) and u = n x (a, b) (n the unit gradient)
-    float acc[M];
+    float acc[FP][M];
 #pragma unroll
-    for (int px = 0; px < M; ++px) acc[px] = 0.f;
+    for (int fr = 0; fr < FP; ++fr)
 #pragma unroll
-    for (int jj = 0; jj < G::W2; ++jj) {
-      const int kyl = 2 * ty + cpy + jj;
-      const float2* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
-      const float2* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
-      float2 sv[G::NQ];
+      for (int px = 0; px < M; ++px) acc[fr][px] = 0.f;
+    if constexpr (FP == 1) {
+      const float2* hg = reinterpret_cast<const float2*>(hgf);
 #pragma unroll
-      for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
-      const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * 3 * G::NS4;
+      for (int jj = 0; jj < G::W2; ++jj) {
+        const int kyl = 2 * ty + cpy + jj;
+        const float2* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
+        const float2* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
+        float2 sv[G::NQ];
 #pragma unroll
-      for (int s4 = 0; s4 < G::NS4; ++s4) {
-        const float4 A = tb[s4];
-        const float4 B = tb[G::NS4 + s4];
-        const float4 Wv = tb[2 * G::NS4 + s4];
+        for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
+        const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * G::TBLK;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int sidx = s4 * 4 + e;
-          if (sidx < G::NS) {
-            const int px = sidx / G::W2;
-            const int ii = sidx % G::W2;
-            const int cpx = (2 * px + 1) / M;
-            const float2 gv = sv[cpx + ii];
-            const float a = f4c(A, e), bb = f4c(B, e), w = f4c(Wv, e);
-            const float dp = fmaf(gv.x, a, gv.y * bb);
-            const float u = fmaf(gv.y, a, -(gv.x * bb));
-            const float v = w - fabsf(u);
-            acc[px] = (dp < 0.f) ? acc[px] + v : acc[px];
+        for (int s4 = 0; s4 < G::NS4; ++s4) {
+          const float4 A = tb[s4];
+          const float4 B = tb[G::NS4 + s4];
+          const float4 Wv = tb[2 * G::NS4 + s4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int sidx = s4 * 4 + e;
+            if (sidx < G::NS) {
+              const int px = sidx / G::W2;
+              const int ii = sidx % G::W2;
+              const int cpx = (2 * px + 1) / M;
+              const float2 gv = sv[cpx + ii];
+              const float a = f4c(A, e), bb = f4c(B, e), w = f4c(Wv, e);
+              const float dp = fmaf(gv.x, a, gv.y * bb);
+              const float u = fmaf(gv.y, a, -(gv.x * bb));
+              const float v = w - fabsf(u);
+              acc[0][px] = (dp < 0.f) ? acc[0][px] + v : acc[0][px];
+            }
+          }
+        }
+      }
+    } else {
+      // frame pair in one register pair: gx = (gx0, gx1), gy = (gy0, gy1)
+      const float4* hg = reinterpret_cast<const float4*>(hgf);
+#pragma unroll
+      for (int jj = 0; jj < G::W2; ++jj) {
+        const int kyl = 2 * ty + cpy + jj;
+        const float4* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
+        const float4* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
+        float4 sv[G::NQ];
+#pragma unroll
+        for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
+        const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * G::TBLK;
+#pragma unroll
+        for (int s4 = 0; s4 < G::NS4; ++s4) {
+          const float4 Wv = tb[6 * G::NS4 + s4];
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 AA = tb[2 * s4 + h];
+            const float4 BB = tb[2 * G::NS4 + 2 * s4 + h];
+            const float4 NB = tb[4 * G::NS4 + 2 * s4 + h];
+#pragma unroll
+            for (int e2 = 0; e2 < 2; ++e2) {
+              const int e = 2 * h + e2;
+              const int sidx = s4 * 4 + e;
+              if (sidx < G::NS) {
+                const int px = sidx / G::W2;
+                const int ii = sidx % G::W2;
+                const int cpx = (2 * px + 1) / M;
+                const float4 g = sv[cpx + ii];
+                const float2 gx = make_float2(g.x, g.y), gy = make_float2(g.z, g.w);
+                const float2 a = e2 ? make_float2(AA.z, AA.w) : make_float2(AA.x, AA.y);
+                const float2 b = e2 ? make_float2(BB.z, BB.w) : make_float2(BB.x, BB.y);
+                const float2 nb = e2 ? make_float2(NB.z, NB.w) : make_float2(NB.x, NB.y);
+                const float w = f4c(Wv, e);
+                const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
+                const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
+                const float v0 = w - fabsf(u.x), v1 = w - fabsf(u.y);
+                acc[0][px] = (dp.x < 0.f) ? acc[0][px] + v0 : acc[0][px];
+                acc[FP - 1][px] = (dp.y < 0.f) ? acc[FP - 1][px] + v1 : acc[FP - 1][px];
+              }
+            }
           }
         }
       }
     }
 
     // ---- epilogue: normalise, ^sensitivity, intensity, margin, temporal ----
-    const float* irow = inten + (ty * M + py) * G::OX + lane * M;
+    const int irow = (ty * M + py) * G::OX + lane * M;
+    const bool first = (fa == f0);
 #pragma unroll
     for (int px = 0; px < M; ++px) {
-      float base = acc[px] * tw[px * G::NT + tid];
-      base = (base < 0.f) ? 0.f : base;
-      const float ival = p.iw ? irow[px] : 1.f;
+      const float twv = tw[px * G::NT + tid];
       const bool zero = (omask & (1u << px)) != 0;
+      float base[FP], ival[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        base[fr] = acc[fr][px] * twv;
+        base[fr] = (base[fr] < 0.f) ? 0.f : base[fr];
+      }
+      if constexpr (FP == 2) {
+        const float2 iv = reinterpret_cast<const float2*>(inten)[irow + px];
+        ival[0] = p.iw ? iv.x : 1.f;
+        ival[FP - 1] = p.iw ? iv.y : 1.f;
+      } else {
+        ival[0] = p.iw ? inten[irow + px] : 1.f;
+      }
       if (MODE == kModeSum) {
         for (int k = 0; k < p.n_sens; ++k) {
-          float r = apply_sens(base, p.sens_mode_k[k], p.sens_int_k[k], p.sens_k[k]);
-          r = zero ? 0.f : r * ival;
           float* K = tk + ((2 * k) * M + px) * G::NT + tid;
           float* S = tk + ((2 * k + 1) * M + px) * G::NT + tid;
-          if (it == 0) {
-            *K = r;
-            *S = 0.f;
-          } else {
-            *S += r - *K;
+          float kv = first ? 0.f : *K, sv = first ? 0.f : *S;
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            if (fr < nf) {
+              float r = apply_sens(base[fr], p.sens_mode_k[k], p.sens_int_k[k], p.sens_k[k]);
+              r = zero ? 0.f : r * ival[fr];
+              if (first && fr == 0) {
+                kv = r;
+                sv = 0.f;
+              } else {
+                sv += r - kv;
+              }
+            }
+          }
+          *K = kv;
+          *S = sv;
+        }
+      } else if (MODE == kModeStack) {
+#pragma unroll
+        for (int fr = 0; fr < FP; ++fr) {
+          if (fr < nf) {
+            float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
+            r = zero ? 0.f : r * ival[fr];
+            if (!(omask >> 31))
+              p.out[(size_t)(fa + fr) * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
           }
         }
       } else {
-        float r = apply_sens(base, p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
-        r = zero ? 0.f : r * ival;
-        if (MODE == kModeStack) {
-          if (!(omask >> 31))
-            p.out[(size_t)f * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
-        } else {
-          float* st = tk + px * G::NT + tid;
-          constexpr int FS = M * G::NT;  // field stride
-          if (it == 0) {
-            st[0] = r;
-            st[FS] = 0.f;
-            st[2 * FS] = 0.f;
-            st[3 * FS] = 0.f;
-            st[4 * FS] = 0.f;
-          } else {
-            const float y = r - st[0];
-            st[FS] += y;
-            st[2 * FS] = fmaf(y, y, st[2 * FS]);
-            st[3 * FS] = fmaf(st[4 * FS], y, st[3 * FS]);
-            st[4 * FS] = y;
+        float* st = tk + px * G::NT + tid;
+        constexpr int FS = M * G::NT;  // field stride
+        float K = 0.f, S = 0.f, Q = 0.f, P = 0.f, L = 0.f;
+        if (!first) {
+          K = st[0];
+          S = st[FS];
+          Q = st[2 * FS];
+          P = st[3 * FS];
+          L = st[4 * FS];
+        }
+#pragma unroll
+        for (int fr = 0; fr < FP; ++fr) {
+          if (fr < nf) {
+            float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
+            r = zero ? 0.f : r * ival[fr];
+            if (first && fr == 0) {
+              K = r;
+            } else {
+              const float y = r - K;
+              S += y;
+              Q = fmaf(y, y, Q);
+              P = fmaf(L, y, P);
+              L = y;
+            }
           }
         }
+        st[0] = K;
+        st[FS] = S;
+        st[2 * FS] = Q;
+        st[3 * FS] = P;
+        st[4 * FS] = L;
       }
     }
   }
 
-  if (abort_it >= 0) {
-    // a TMA tile never arrived: wait (bounded) for the copies still in flight
-    // (this frame's and the next one's), then leave without writing
+  if (aborted) {
+    // a TMA tile never arrived: wait (bounded) for the copies still in flight,
+    // then leave without writing
     if (tid == 0) {
-      const int bb = abort_it & 1;
-      (void)mbar_wait_bounded(&bar[bb], (bb ? ph1 : ph0) & 1u);
-      if (f0 + abort_it + 1 < f1)
-        (void)mbar_wait_bounded(&bar[bb ^ 1], (bb ? ph0 : ph1) & 1u);
+      for (int k = 0; k < 2 * FP; ++k)
+        if (pend & (1u << k)) (void)mbar_wait_bounded(&bar[k], (phase >> k) & 1u);
     }
     return;
   }
@@ -613,29 +826,25 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   }  // unit loop
 }
 
-constexpr size_t kMaxSmemPerBlock = 227 * 1024;
-
 template <int M, int J, int MODE>
 size_t fused_smem_bytes(int ns_cap) {
-  constexpr int TY = TileRows<M>::TY;
-  return Geo<M, J, TY>::smem_bytes(MODE, ns_cap);
+  return FusedCfg<M, J, MODE>::G::smem_bytes(MODE, ns_cap);
 }
 
 template <int M, int J, int MODE>
 cudaError_t launch_fused(const UnitTable& ut, const TmapPack& maps, int grid,
                          cudaStream_t stream) {
-  constexpr int TY = TileRows<M>::TY;
-  using G = Geo<M, J, TY>;
-  auto kern = esrrf_fused_kernel<M, J, TY, MODE>;
+  using C = FusedCfg<M, J, MODE>;
+  using G = typename C::G;
+  auto kern = esrrf_fused_kernel<M, J, C::TY, C::FP, MODE>;
   const size_t smem = G::smem_bytes(MODE, MODE == kModeSum ? ut.ns_cap : 1);
-  if (smem + sizeof(FusedParams) + 64 > kMaxSmemPerBlock) return cudaErrorInvalidValue;
+  if (smem > kSmemBudget) return cudaErrorInvalidValue;
   static int attr_done = -1;  // device the attributes were last set for
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (attr_done != dev) {
-    const size_t cap = std::min(kMaxSmemPerBlock - sizeof(FusedParams) - 64,
-                                G::smem_bytes(MODE, MODE == kModeSum ? kMaxSens : 1));
+    const size_t cap = std::min(kSmemBudget, G::smem_bytes(MODE, C::NSC));
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -651,32 +860,31 @@ cudaError_t launch_fused(const UnitTable& ut, const TmapPack& maps, int grid,
 // resident CTAs per SM of one instantiation (for persistent grids)
 template <int M, int J, int MODE>
 int fused_occupancy(int ns_cap) {
-  constexpr int TY = TileRows<M>::TY;
-  using G = Geo<M, J, TY>;
+  using C = FusedCfg<M, J, MODE>;
+  using G = typename C::G;
+  auto kern = esrrf_fused_kernel<M, J, C::TY, C::FP, MODE>;
   const size_t smem = G::smem_bytes(MODE, MODE == kModeSum ? ns_cap : 1);
-  if (smem + sizeof(FusedParams) + 64 > kMaxSmemPerBlock) return 0;
+  if (smem > kSmemBudget) return 0;
   int n = 0;
-  const size_t cap = std::min(kMaxSmemPerBlock - sizeof(FusedParams) - 64,
-                              G::smem_bytes(MODE, MODE == kModeSum ? kMaxSens : 1));
-  if (cudaFuncSetAttribute(esrrf_fused_kernel<M, J, TY, MODE>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap) != cudaSuccess)
+  const size_t cap = std::min(kSmemBudget, G::smem_bytes(MODE, C::NSC));
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cap) !=
+      cudaSuccess)
     return 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, esrrf_fused_kernel<M, J, TY, MODE>, G::NT,
-                                                    smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, G::NT, smem) != cudaSuccess)
     return 1;
   return n > 0 ? n : 1;
 }
 
-// geometry the host needs to build the tensor map for a given (M, J)
+// geometry the host needs to build the tensor map for a given (M, J); the
+// tile shape does not depend on the mode or on FP
 struct FusedGeometry {
   int TY, IX, IY, BW, BH;
 };
 
 template <int M, int J>
 FusedGeometry fused_geometry() {
-  constexpr int TY = TileRows<M>::TY;
-  using G = Geo<M, J, TY>;
-  return FusedGeometry{TY, G::IX, G::IY, G::BW, G::BH};
+  using G = Geo<M, J, TileRows<M>::TY, 1>;
+  return FusedGeometry{TileRows<M>::TY, G::IX, G::IY, G::BW, G::BH};
 }
 
 }  // namespace nx
