@@ -69,6 +69,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
 // Wait for phase `parity` of `bar`; gives up after `limit_ns` and returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity,
                                                   unsigned long long limit_ns = kWaitLimitNs) {
@@ -76,6 +81,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   const unsigned long long t0 = global_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
+// As mbar_wait_bounded, but also gives up as soon as *abort is set (another
+// thread of the CTA gave up first), so that no thread waits for an arrival
+// that will never come.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, unsigned parity,
+                                                   const volatile int* abort,
+                                                   unsigned long long limit_ns = kWaitLimitNs) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (true) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
     if (global_ns() - t0 > limit_ns) return false;
   }
 }

@@ -1,4 +1,4 @@
-// Fused eSRRF frame-loop kernel (sm_103a).
+// Fused eSRRF frame-loop kernel (sm_103a), warp-specialised.
 //
 // One CTA owns a 32 x TY tile of input pixels (= a 32M x TY*M tile of output
 // pixels), one timepoint and one contiguous chunk of that timepoint's frames.
@@ -88,11 +88,29 @@ struct TileRows {
   static constexpr int TY = (M <= 2) ? 8 : (M <= 5 ? 4 : 2);
 };
 
-// Frames per pass (FP).  With FP = 2 a thread carries two consecutive frames
-// through each pass of the frame loop: the RGC core runs on packed f32x2
-// arithmetic (frame pair in one register pair, one phase-table load for both
-// frames) and the preparation shares its index and weight work.  Results are
-// bit-identical to FP = 1 (the same IEEE operations per frame).
+// Warp roles of the eSRRF kernel.  Each CTA runs 32 * TY * M consumer threads
+// (one per input pixel and output row phase: RGC, normalisation, temporal
+// update) and one producer warpgroup that prepares the gradient and intensity
+// tiles of the next frames (TMA, Roberts-Cross, Catmull-Rom passes,
+// normalisation) into a double-buffered slot while the consumers work on the
+// current one.  The consumers' RGC is FMA-pipe bound and the preparation is
+// load/ALU bound, so the two overlap on the SM.
+template <int M>
+struct EsrrfTile {
+  // rows per tile: as many consumer warps as the registers allow without
+  // spilling (m = 5: 20 consumer + 4 producer warps at 80 registers measured
+  // 12 % faster than 15 + 4 at 96, 40 % faster than 10 + 4)
+  static constexpr int TY = (M <= 2) ? 8 : (M <= 3 ? 4 : (M == 4 ? 3 : (M == 5 ? 4 : (M == 6 ? 2 : 1))));
+  static constexpr int NT = 32 * TY * M + 128;
+  static constexpr int MIN_BLOCKS = (M <= 2 && NT <= 384) ? 2 : 1;
+};
+constexpr int kProducerThreads = 128;  // one warpgroup (96 or 64 measured slower)
+
+// Frames per pass (FP).  With FP = 2 a consumer carries two consecutive frames
+// through each pass: the RGC core runs on packed f32x2 arithmetic (frame pair
+// in one register pair, one phase-table load for both frames) and the
+// producers share their index and weight work between the two frames.
+// Results are bit-identical to FP = 1 (the same IEEE operations per frame).
 // Instantiations whose FP = 2 shared-memory layout does not fit a CTA use FP = 1.
 template <int M, int J, int TY, int FP>
 struct Geo {
@@ -117,7 +135,9 @@ struct Geo {
   static constexpr int OY = TY * M;
   static constexpr int OX = TX * M;
   static constexpr int RIW = TX + 4;
-  static constexpr int NT = 32 * TY * M;
+  static constexpr int NTC = 32 * TY * M;        // consumer threads
+  static constexpr int NP = kProducerThreads;    // producer threads
+  static constexpr int NT = NTC + NP;
   // phase-table block per (py, jj), in float4:
   //   FP = 1: a[NS4] b[NS4] w[NS4]   (4 samples per float4)
   //   FP = 2: (a, b, -b, w) per sample, each value broadcast into a frame pair
@@ -133,27 +153,28 @@ struct Geo {
   static constexpr int O_T1 = O_G + 2 * FP * S_G;
   static constexpr int S_T1 = al(NRY * HG_C);  // column-pass gx, gy per frame
   static constexpr int O_HG = O_T1 + 2 * FP * S_T1;
-  static constexpr int S_HG = al(HG_R * 2 * HGP * 2 * FP);  // unit gradients: float2 / float4
-  static constexpr int O_RI = O_HG + S_HG;
+  static constexpr int S_HG = al(HG_R * 2 * HGP * 2 * FP);  // one slot: float2 / float4 gradients
+  static constexpr int O_RI = O_HG + 2 * S_HG;              // two slots
   static constexpr int S_RI = al(OY * RIW);  // intensity row pass per frame
-  static constexpr int O_TB = O_RI + FP * S_RI;
+  static constexpr int O_TB = O_RI + 2 * FP * S_RI;         // two slots of FP planes
   static constexpr int S_TB = al(M * W2 * TBLK * 4);
   static constexpr int O_RW = O_TB + S_TB;
   static constexpr int S_RW = al(OY * 5);
   static constexpr int O_CW = O_RW + S_RW;
   static constexpr int S_CW = al(OX * 5);
-  // per-output temporal state kept out of registers, [px][thread] planes:
+  // per-output temporal state kept out of registers, [px][consumer] planes:
   //   FULL: float4 (K, S, Q, P) then float L;  SUM: float2 (K, S) per sensitivity
-  static constexpr int O_TW = O_CW + S_CW;    // 1 / sum w per output
-  static constexpr int O_TK = O_TW + M * NT;
-  static constexpr int S_TK_FULL = 5 * M * NT;
+  static constexpr int O_TW = O_CW + S_CW;     // 1 / sum w per output
+  static constexpr int O_TK = O_TW + M * NTC;
+  static constexpr int S_TK_FULL = 5 * M * NTC;
   static constexpr int O_BAR_FULL = O_TK + S_TK_FULL;
   // AVG mode keeps K and S of ns_cap sensitivities per output
   __host__ __device__ static constexpr int o_bar(int mode, int ns_cap) {
-    return mode == 1 ? O_TK + 2 * ns_cap * M * NT : (mode == 2 ? O_BAR_FULL : O_TK);
+    return mode == 1 ? O_TK + 2 * ns_cap * M * NTC : (mode == 2 ? O_BAR_FULL : O_TK);
   }
+  // 5 + 2 FP mbarriers after o_bar
   __host__ __device__ static constexpr size_t smem_bytes(int mode, int ns_cap) {
-    return size_t(o_bar(mode, ns_cap) + 32 + 64) * 4;
+    return size_t(o_bar(mode, ns_cap) + 32) * 4;
   }
 };
 
@@ -163,7 +184,7 @@ constexpr size_t kSmemBudget = kMaxSmemPerBlock - sizeof(FusedParams) - 64;
 // compile-time configuration of one instantiation
 template <int M, int J, int MODE>
 struct FusedCfg {
-  static constexpr int TY = TileRows<M>::TY;
+  static constexpr int TY = EsrrfTile<M>::TY;
   static constexpr int NSC = MODE == kModeSum ? kMaxSens : 1;
   static constexpr int FP = Geo<M, J, TY, 2>::smem_bytes(MODE, NSC) <= kSmemBudget ? 2 : 1;
   using G = Geo<M, J, TY, FP>;
@@ -183,38 +204,321 @@ __device__ __forceinline__ float apply_sens(float r, int mode, int n, float s) {
   return r;
 }
 
+// geometry of one unit (tile, timepoint, frame chunk), shared by both roles
+struct UnitGeo {
+  int nx0, ny0, H, W, f0, f1;
+  int kb_y, kb_x, RY0, CX0, y_start, x_start, kmax_y, kmax_x;
+};
+
+// ---------------------------------------------------------------------------
+// producer warpgroup: input tiles -> slot s (unit gradients hg, intensity rows ri)
+// ---------------------------------------------------------------------------
+template <int M, int J, int TY, int FP>
+struct Producer {
+  using G = Geo<M, J, TY, FP>;
+  float* inb;
+  float* gsm;  // plane 2 fr: gc, 2 fr + 1: gr
+  float* t1;   // plane 2 fr: gx, 2 fr + 1: gy (half-grid columns)
+  float* hg0;  // slot 0; slot s at hg0 + s * S_HG
+  float* ri0;  // slot s, frame fr at ri0 + (s * FP + fr) * S_RI
+  const float* rw;
+  int ptid;
+
+  __device__ void roberts_and_rows(const FusedParams& p, const UnitGeo& u, const float* const* tin,
+                                   int s) const {
+    for (int i = ptid; i < G::NRY * G::NCX; i += G::NP) {
+      const int rl = i / G::NCX, cl = i % G::NCX;
+      const int r = u.RY0 + rl, c = u.CX0 + cl;
+      const bool in = r >= 0 && r < u.H && c >= 0 && c < u.W;
+      const int r0 = r > 0 ? r - 1 : 0;
+      const int c0 = c > 0 ? c - 1 : 0;
+      const int ia = (r0 - u.y_start) * G::BW + (c - u.x_start);   // image[r0][c1]
+      const int ib = (r - u.y_start) * G::BW + (c0 - u.x_start);   // image[r1][c0]
+      const int id = (r0 - u.y_start) * G::BW + (c0 - u.x_start);  // image[r0][c0]
+      const int ie = (r - u.y_start) * G::BW + (c - u.x_start);    // image[r1][c1]
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        float gc = 0.f, gr = 0.f;
+        if (in) {
+          const float a = tin[fr][ia], bb = tin[fr][ib], d = tin[fr][id], e = tin[fr][ie];
+          gc = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
+          gr = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
+        }
+        gsm[(2 * fr) * G::S_G + i] = gc;
+        gsm[(2 * fr + 1) * G::S_G + i] = gr;
+      }
+    }
+    float* ri = ri0 + s * FP * G::S_RI;
+    for (int i = ptid; i < G::OY * G::RIW; i += G::NP) {
+      const int oy = i / G::RIW, cc = i % G::RIW;
+      const int nyo = u.ny0 + oy / M;
+      float w5[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) w5[k] = rw[oy * 5 + k];
+      const int off = (nyo - 2 - u.y_start) * G::BW + (u.nx0 - 2 + cc - u.x_start);
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        const float* col = tin[fr] + off;
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) sum = fmaf(w5[k], col[k * G::BW], sum);
+        ri[fr * G::S_RI + i] = sum;
+      }
+    }
+  }
+
+  // gradient column pass onto the half-grid columns
+  __device__ void column_pass(const FusedParams& p, const UnitGeo& u) const {
+    const int twoW = 2 * u.W;
+    for (int i = ptid; i < G::NRY * G::HG_C; i += G::NP) {
+      const int rl = i / G::HG_C, kxl = i % G::HG_C;
+      const int kx = u.kb_x + kxl;
+      float vc[FP], vr[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) vc[fr] = vr[fr] = 0.f;
+      if (kx >= 1 && kx <= u.kmax_x) {
+        if (kx >= twoW) {
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX;
+            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int cl = p.cx_base + t - u.CX0;
+              vc[fr] = fmaf(p.cx[t], g0[cl], vc[fr]);
+              vr[fr] = fmaf(p.cx[t], g1[cl], vr[fr]);
+            }
+          }
+        } else if (kx & 1) {
+          const int cl = ((kx - 1) >> 1) - u.CX0;
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            vc[fr] = gsm[(2 * fr) * G::S_G + rl * G::NCX + cl];
+            vr[fr] = gsm[(2 * fr + 1) * G::S_G + rl * G::NCX + cl];
+          }
+        } else {
+          const int cl = (kx >> 1) - 2 - u.CX0;
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX + cl;
+            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX + cl;
+            float c = -0.0625f * g0[0], r = -0.0625f * g1[0];
+            c = fmaf(0.5625f, g0[1], c);
+            r = fmaf(0.5625f, g1[1], r);
+            c = fmaf(0.5625f, g0[2], c);
+            r = fmaf(0.5625f, g1[2], r);
+            vc[fr] = fmaf(-0.0625f, g0[3], c);
+            vr[fr] = fmaf(-0.0625f, g1[3], r);
+          }
+        }
+      }
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) {
+        t1[(2 * fr) * G::S_T1 + i] = vc[fr];
+        t1[(2 * fr + 1) * G::S_T1 + i] = vr[fr];
+      }
+    }
+  }
+
+  // gradient row pass and normalisation -> unit gradients of slot s
+  __device__ void row_pass(const FusedParams& p, const UnitGeo& u, int s) const {
+    const int twoH = 2 * u.H;
+    float* hgf = hg0 + s * G::S_HG;
+    for (int i = ptid; i < G::HG_R * G::HG_C; i += G::NP) {
+      const int kyl = i / G::HG_C, kxl = i % G::HG_C;
+      const int ky = u.kb_y + kyl, kx = u.kb_x + kxl;
+      float nxv[FP], nyv[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) nxv[fr] = nyv[fr] = 0.f;
+      if (ky >= 1 && ky <= u.kmax_y && kx >= 1 && kx <= u.kmax_x) {
+        float gx[FP], gy[FP];
+        if (ky >= twoH) {
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* c0 = t1 + (2 * fr) * G::S_T1 + kxl;
+            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + kxl;
+            gx[fr] = gy[fr] = 0.f;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int rl = p.cy_base + t - u.RY0;
+              gx[fr] = fmaf(p.cy[t], c0[rl * G::HG_C], gx[fr]);
+              gy[fr] = fmaf(p.cy[t], c1[rl * G::HG_C], gy[fr]);
+            }
+          }
+        } else if (ky & 1) {
+          const int rl = ((ky - 1) >> 1) - u.RY0;
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            gx[fr] = t1[(2 * fr) * G::S_T1 + rl * G::HG_C + kxl];
+            gy[fr] = t1[(2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl];
+          }
+        } else {
+          const int rl = (ky >> 1) - 2 - u.RY0;
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            const float* c0 = t1 + (2 * fr) * G::S_T1 + rl * G::HG_C + kxl;
+            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl;
+            float x = -0.0625f * c0[0], y = -0.0625f * c1[0];
+            x = fmaf(0.5625f, c0[G::HG_C], x);
+            y = fmaf(0.5625f, c1[G::HG_C], y);
+            x = fmaf(0.5625f, c0[2 * G::HG_C], x);
+            y = fmaf(0.5625f, c1[2 * G::HG_C], y);
+            gx[fr] = fmaf(-0.0625f, c0[3 * G::HG_C], x);
+            gy[fr] = fmaf(-0.0625f, c1[3 * G::HG_C], y);
+          }
+        }
+#pragma unroll
+        for (int fr = 0; fr < FP; ++fr) {
+          const float m2 = fmaf(gx[fr], gx[fr], gy[fr] * gy[fr]);
+          if (m2 > 0.f) {
+            const float inv = rsqrtf(m2);
+            nxv[fr] = gx[fr] * inv;
+            nyv[fr] = gy[fr] * inv;
+          }
+        }
+      }
+      const int o = (kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1);
+      if constexpr (FP == 2)
+        reinterpret_cast<float4*>(hgf)[o] = make_float4(nxv[0], nxv[1], nyv[0], nyv[1]);
+      else
+        reinterpret_cast<float2*>(hgf)[o] = make_float2(nxv[0], nyv[0]);
+    }
+  }
+};
+
+// RGC of one consumer's M outputs for the FP frames of slot hgf.
+// Contribution of sample (phase, offset): (dp < 0) ? w - |u| : 0 with
+// dp = n.(a, b) and u = n x (a, b) (n the unit gradient).
+template <int M, int J, int TY, int FP>
+__device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, int ty, int py,
+                                         int lane, float (&acc)[FP][M]) {
+  using G = Geo<M, J, TY, FP>;
+  const int cpy = (2 * py + 1) / M;
+#pragma unroll
+  for (int fr = 0; fr < FP; ++fr)
+#pragma unroll
+    for (int px = 0; px < M; ++px) acc[fr][px] = 0.f;
+  if constexpr (FP == 1) {
+    const float2* hg = reinterpret_cast<const float2*>(hgf);
+#pragma unroll
+    for (int jj = 0; jj < G::W2; ++jj) {
+      const int kyl = 2 * ty + cpy + jj;
+      const float2* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
+      const float2* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
+      float2 sv[G::NQ];
+#pragma unroll
+      for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
+      const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * G::TBLK;
+#pragma unroll
+      for (int s4 = 0; s4 < G::NS4; ++s4) {
+        const float4 A = tb[s4];
+        const float4 B = tb[G::NS4 + s4];
+        const float4 Wv = tb[2 * G::NS4 + s4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int sidx = s4 * 4 + e;
+          if (sidx < G::NS) {
+            const int px = sidx / G::W2;
+            const int ii = sidx % G::W2;
+            const int cpx = (2 * px + 1) / M;
+            const float2 gv = sv[cpx + ii];
+            const float a = f4c(A, e), bb = f4c(B, e), w = f4c(Wv, e);
+            const float dp = fmaf(gv.x, a, gv.y * bb);
+            const float u = fmaf(gv.y, a, -(gv.x * bb));
+            const float v = w - fabsf(u);
+            acc[0][px] = (dp < 0.f) ? acc[0][px] + v : acc[0][px];
+          }
+        }
+      }
+    }
+  } else {
+    // frame pair in one register pair: gx = (gx0, gx1), gy = (gy0, gy1); every
+    // FMA-pipe operation is packed: v = w + (-|u|), acc += [dp < 0] * v
+    // (measured 6 % faster than scalar v and predicated scalar adds)
+    const float4* hg = reinterpret_cast<const float4*>(hgf);
+    float2 acc2[M];
+#pragma unroll
+    for (int px = 0; px < M; ++px) acc2[px] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int jj = 0; jj < G::W2; ++jj) {
+      const int kyl = 2 * ty + cpy + jj;
+      const float4* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
+      const float4* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
+      float4 sv[G::NQ];
+#pragma unroll
+      for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
+      const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * G::TBLK;
+#pragma unroll
+      for (int sidx = 0; sidx < G::NS; ++sidx) {
+        const int px = sidx / G::W2;
+        const int ii = sidx % G::W2;
+        const int cpx = (2 * px + 1) / M;
+        const float4 g = sv[cpx + ii];
+        const float2 gx = make_float2(g.x, g.y), gy = make_float2(g.z, g.w);
+        const float4 T = tb[sidx];
+        const float2 a = make_float2(T.x, T.x), b = make_float2(T.y, T.y);
+        const float2 nb = make_float2(T.z, T.z);
+        const float w = T.w;
+        const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
+        const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
+        const float2 nu = make_float2(__int_as_float(__float_as_int(u.x) | 0x80000000),
+                                      __int_as_float(__float_as_int(u.y) | 0x80000000));
+        const float2 v = __fadd2_rn(make_float2(w, w), nu);
+        const float2 msk = make_float2(dp.x < 0.f ? 1.f : 0.f, dp.y < 0.f ? 1.f : 0.f);
+        acc2[px] = __ffma2_rn(msk, v, acc2[px]);
+      }
+    }
+#pragma unroll
+    for (int px = 0; px < M; ++px) {
+      acc[0][px] = acc2[px].x;
+      acc[FP - 1][px] = acc2[px].y;
+    }
+  }
+}
+
 template <int M, int J, int TY, int FP, int MODE>
-__global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
+__global__ void __launch_bounds__(32 * TY * M + kProducerThreads, EsrrfTile<M>::MIN_BLOCKS)
     esrrf_fused_kernel(const __grid_constant__ TmapPack maps, const UnitTable ut) {
   using G = Geo<M, J, TY, FP>;
   extern __shared__ __align__(128) float sm[];
   __shared__ FusedParams sp;
   __shared__ int s_unit;
-  float* inb = sm + G::O_INB;
-  float* gsm = sm + G::O_G;   // plane 2 fr: gc, 2 fr + 1: gr
-  float* t1 = sm + G::O_T1;   // plane 2 fr: gx, 2 fr + 1: gy (half-grid columns)
-  float* hgf = sm + G::O_HG;  // FP = 1: float2 (nx, ny); FP = 2: float4 (nx0, nx1, ny0, ny1)
-  float* ri = sm + G::O_RI;   // plane fr
+  __shared__ int s_abort;
   float4* tb4 = reinterpret_cast<float4*>(sm + G::O_TB);
   float* rw = sm + G::O_RW;
   float* cw = sm + G::O_CW;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + G::o_bar(MODE, ut.ns_cap));
-  float* tw = sm + G::O_TW;  // tw[px * NT + tid]
+  float* tw = sm + G::O_TW;  // tw[px * NTC + tid]
   float* tk = sm + G::O_TK;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + G::o_bar(MODE, ut.ns_cap));
+  uint64_t* full = bars;       // [2] slot prepared (NP arrivals)
+  uint64_t* empty = bars + 2;  // [2] slot released (NTC arrivals)
+  uint64_t* pbar = bars + 4;   // producer-group barrier (NP arrivals)
+  uint64_t* tbar = bars + 5;   // [2 FP] TMA input tiles
 
   const int tid = threadIdx.x;
+  const bool producer = tid >= G::NTC;
   const int lane = tid & 31;
   const int warp = tid >> 5;
-  const int ty = warp % TY;
+  const int ty = warp % TY;  // consumers
   const int py = warp / TY;
+  Producer<M, J, TY, FP> prod{sm + G::O_INB, sm + G::O_G, sm + G::O_T1, sm + G::O_HG,
+                              sm + G::O_RI, rw, tid - G::NTC};
 
   if (tid == 0) {
-    for (int k = 0; k < 2 * FP; ++k) mbar_init(&bar[k], 1);
+    mbar_init(&full[0], G::NP);
+    mbar_init(&full[1], G::NP);
+    mbar_init(&empty[0], G::NTC);
+    mbar_init(&empty[1], G::NTC);
+    mbar_init(pbar, G::NP);
+    for (int k = 0; k < 2 * FP; ++k) mbar_init(&tbar[k], 1);
     fence_mbar_init();
+    s_abort = 0;
   }
   __syncthreads();
-  unsigned phase = 0;  // bit k: parity of the next completion of bar[k] (same in every thread)
-  unsigned pend = 0;   // bit k: a TMA load into input buffer k is in flight
+  unsigned gp = 0;      // frame passes since launch: slot gp & 1, use gp >> 1 (all threads)
+  unsigned tphase = 0;  // producers: bit k = parity of the next completion of tbar[k]
+  unsigned tpend = 0;   // producers: bit k = a TMA load into input buffer k is in flight
+  unsigned pphase = 0;  // producers: parity of the next completion of pbar
   int cur_item = -1;
 
   for (int iter = 0;; ++iter) {
@@ -262,548 +566,336 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
   const int tile = local % tiles;
   const int tp = (local / tiles) / p.chunks;
   const int chunk = (local / tiles) % p.chunks;
-  const int tile_x = tile % p.tiles_x;
-  const int tile_y = tile / p.tiles_x;
-  const int nx0 = tile_x * G::TX;
-  const int ny0 = tile_y * TY;
-  const int H = p.H, W = p.W;
 
   // frames of this unit
   const int tp_f0 = tp * p.fpt;
   const int tp_nf = min(p.fpt, p.T - tp_f0);
   const int nch = min(p.chunks, tp_nf);
+  int npass = 0;
   if (chunk < nch) {  // uniform across the CTA
-  const int f0 = tp_f0 + (int)((long long)chunk * tp_nf / nch);
-  const int f1 = tp_f0 + (int)((long long)(chunk + 1) * tp_nf / nch);
-
-  const int kb_y = 2 * ny0 - J;
-  const int kb_x = 2 * nx0 - J;
-  const int RY0 = ny0 - G::RLO;
-  const int CX0 = nx0 - G::CLO;
-  const int y_start = ny0 - G::IY;
-  const int x_start = nx0 - G::IX;
-  const int twoH = 2 * H, twoW = 2 * W;
-  const int kmax_y = 2 * p.rowsM - 2, kmax_x = 2 * p.colsM - 2;
+  UnitGeo u;
+  u.nx0 = (tile % p.tiles_x) * G::TX;
+  u.ny0 = (tile / p.tiles_x) * TY;
+  u.H = p.H;
+  u.W = p.W;
+  u.f0 = tp_f0 + (int)((long long)chunk * tp_nf / nch);
+  u.f1 = tp_f0 + (int)((long long)(chunk + 1) * tp_nf / nch);
+  u.kb_y = 2 * u.ny0 - J;
+  u.kb_x = 2 * u.nx0 - J;
+  u.RY0 = u.ny0 - G::RLO;
+  u.CX0 = u.nx0 - G::CLO;
+  u.y_start = u.ny0 - G::IY;
+  u.x_start = u.nx0 - G::IX;
+  u.kmax_y = 2 * p.rowsM - 2;
+  u.kmax_x = 2 * p.colsM - 2;
+  const int f0 = u.f0, f1 = u.f1;
+  npass = (f1 - f0 + FP - 1) / FP;
 
   // ---- per-CTA constants: intensity interpolation weights -----------------
-  {
-    for (int i = tid; i < G::OY; i += G::NT) {
-      const int yM = ny0 * M + i;
-      const int ny = ny0 + i / M;
-      const float ry = __fdiv_rn((float)yM, (float)M);
-      const int rb = (int)floorf(ry - 0.5f);
-      float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = tid; i < G::OY; i += G::NT) {
+    const int yM = u.ny0 * M + i;
+    const int nyp = u.ny0 + i / M;
+    const float ry = __fdiv_rn((float)yM, (float)M);
+    const int rb = (int)floorf(ry - 0.5f);
+    float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int nb = rb - 1 + t;
-        const int k = nb - (ny - 2);
-        const float w = cr_cubic(ry - ((float)nb + 0.5f));
+    for (int t = 0; t < 4; ++t) {
+      const int nb = rb - 1 + t;
+      const int k = nb - (nyp - 2);
+      const float w = cr_cubic(ry - ((float)nb + 0.5f));
 #pragma unroll
-        for (int kk = 0; kk < 5; ++kk) w5[kk] = (k == kk) ? w : w5[kk];
-      }
-#pragma unroll
-      for (int k = 0; k < 5; ++k) rw[i * 5 + k] = w5[k];
+      for (int kk = 0; kk < 5; ++kk) w5[kk] = (k == kk) ? w : w5[kk];
     }
-    for (int i = tid; i < G::OX; i += G::NT) {
-      const int xM = nx0 * M + i;
-      const int nxp = nx0 + i / M;
-      const float rx = __fdiv_rn((float)xM, (float)M);
-      const int cb = (int)floorf(rx - 0.5f);
-      float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int nb = cb - 1 + t;
-        const int k = nb - (nxp - 2);
-        const float w = cr_cubic(rx - ((float)nb + 0.5f));
+    for (int k = 0; k < 5; ++k) rw[i * 5 + k] = w5[k];
+  }
+  for (int i = tid; i < G::OX; i += G::NT) {
+    const int xM = u.nx0 * M + i;
+    const int nxp = u.nx0 + i / M;
+    const float rx = __fdiv_rn((float)xM, (float)M);
+    const int cb = (int)floorf(rx - 0.5f);
+    float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int kk = 0; kk < 5; ++kk) w5[kk] = (k == kk) ? w : w5[kk];
-      }
+    for (int t = 0; t < 4; ++t) {
+      const int nb = cb - 1 + t;
+      const int k = nb - (nxp - 2);
+      const float w = cr_cubic(rx - ((float)nb + 0.5f));
 #pragma unroll
-      for (int k = 0; k < 5; ++k) cw[i * 5 + k] = w5[k];
+      for (int kk = 0; kk < 5; ++kk) w5[kk] = (k == kk) ? w : w5[kk];
     }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) cw[i * 5 + k] = w5[k];
   }
 
-  // ---- per-thread constants ------------------------------------------------
-  const int ny = ny0 + ty;
-  const int nx = nx0 + lane;
+  // ---- consumer constants --------------------------------------------------
+  const int ny = u.ny0 + ty;
+  const int nx = u.nx0 + lane;
   const int yM = ny * M + py;
-  const int cpy = (2 * py + 1) / M;
-  unsigned omask = 0;  // bit px: output forced to 0 / not written
-  {
+  unsigned omask = 0;  // bit px: output forced to 0 / not written; bit 31: outside the image
+  if (!producer) {
+    const int cpy = (2 * py + 1) / M;
     const int ky_lo = 2 * ny + cpy - J, ky_hi = 2 * ny + cpy + J;
-    const bool by = (ky_lo < 1) || (ky_hi > kmax_y);
+    const bool by = (ky_lo < 1) || (ky_hi > u.kmax_y);
 #pragma unroll
     for (int px = 0; px < M; ++px) {
       const int cpx = (2 * px + 1) / M;
       const int xM = nx * M + px;
       const int kx_lo = 2 * nx + cpx - J, kx_hi = 2 * nx + cpx + J;
       float iw = p.inv_wsum[py * M + px];
-      if (by || kx_lo < 1 || kx_hi > kmax_x) {
+      if (by || kx_lo < 1 || kx_hi > u.kmax_x) {
         // window reaches invalid half-grid samples: they count in neither sum
         const float* wf = p.wfull + (size_t)(py * M + px) * G::W2 * G::W2;
         float s = 0.f;
         for (int jj = 0; jj < G::W2; ++jj) {
           const int ky = ky_lo + jj;
-          if (ky < 1 || ky > kmax_y) continue;
+          if (ky < 1 || ky > u.kmax_y) continue;
           for (int ii = 0; ii < G::W2; ++ii) {
             const int kx = kx_lo + ii;
-            if (kx < 1 || kx > kmax_x) continue;
+            if (kx < 1 || kx > u.kmax_x) continue;
             s += wf[jj * G::W2 + ii];
           }
         }
         iw = s > 0.f ? 1.f / s : 0.f;
       }
-      tw[px * G::NT + tid] = iw;
-      const bool outside = (ny >= H) || (nx >= W);
+      tw[px * G::NTC + tid] = iw;
+      const bool outside = (ny >= u.H) || (nx >= u.W);
       const bool in_margin = (yM < p.margin) || (yM >= p.rowsM - p.margin) ||
                              (xM < p.margin) || (xM >= p.colsM - p.margin);
       if (outside) omask |= (1u << px) | (1u << 31);
       else if (in_margin) omask |= (1u << px);
     }
   }
-
-  constexpr unsigned kTileBytes = unsigned(G::BH * G::BW * 4);
-  const bool use_tma = p.tmap >= 0;
-  const CUtensorMap* tmap = use_tma ? &maps.m[p.tmap] : nullptr;
   __syncthreads();
-  if (use_tma) {
-    // input buffer k = set * FP + fr holds frame f0 + k for the first two sets
-    if (tid == 0) fence_proxy_async_smem();
-    for (int k = 0; k < 2 * FP; ++k) {
-      if (f0 + k < f1) {
-        if (tid == 0) {
-          mbar_arrive_expect_tx(&bar[k], kTileBytes);
-          tma_load_3d(inb + k * G::S_INB, tmap, &bar[k], x_start, y_start, f0 + k);
-        }
-        pend |= 1u << k;
-      }
-    }
-  }
 
-  const size_t plane = (size_t)p.rowsM * p.colsM;
-  bool aborted = false;
-
-  for (int fa = f0; fa < f1; fa += FP) {
-    const int set = ((fa - f0) / FP) & 1;
-    const int nf = min(FP, f1 - fa);  // frames of this pass (the last pass may hold one)
-    const float* tin[FP];
-#pragma unroll
-    for (int fr = 0; fr < FP; ++fr)
-      tin[fr] = inb + (set * FP + (fr < nf ? fr : 0)) * G::S_INB;
-    if (use_tma) {
-      bool ok = true;
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        const int k = set * FP + fr;
-        if (fr < nf && ok) {
-          ok = mbar_wait_bounded(&bar[k], (phase >> k) & 1u);
-          if (ok) {
-            phase ^= 1u << k;
-            pend &= ~(1u << k);
-          }
-        }
-      }
-      if (__syncthreads_or(!ok)) {
-        if (tid == 0) atomicOr(p.status, kDevTmaTimeout);
-        aborted = true;
-        break;
-      }
-    } else {
-      for (int fr = 0; fr < nf; ++fr) {
-        const float* src = p.in + (size_t)(fa + fr) * H * W;
-        float* dst = inb + (set * FP + fr) * G::S_INB;
-        for (int i = tid; i < G::BH * G::BW; i += G::NT) {
-          const int r = y_start + i / G::BW;
-          const int c = x_start + i % G::BW;
-          dst[i] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(src + (size_t)r * W + c) : 0.f;
-        }
-      }
-      __syncthreads();
-    }
-
-    // ---- phase 1: Roberts-Cross, intensity row pass --------------------
-    for (int i = tid; i < G::NRY * G::NCX; i += G::NT) {
-      const int rl = i / G::NCX, cl = i % G::NCX;
-      const int r = RY0 + rl, c = CX0 + cl;
-      const bool in = r >= 0 && r < H && c >= 0 && c < W;
-      const int r0 = r > 0 ? r - 1 : 0;
-      const int c0 = c > 0 ? c - 1 : 0;
-      const int ia = (r0 - y_start) * G::BW + (c - x_start);   // image[r0][c1]
-      const int ib = (r - y_start) * G::BW + (c0 - x_start);   // image[r1][c0]
-      const int id = (r0 - y_start) * G::BW + (c0 - x_start);  // image[r0][c0]
-      const int ie = (r - y_start) * G::BW + (c - x_start);    // image[r1][c1]
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        float gc = 0.f, gr = 0.f;
-        if (in) {
-          const float a = tin[fr][ia], bb = tin[fr][ib], d = tin[fr][id], e = tin[fr][ie];
-          gc = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
-          gr = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
-        }
-        gsm[(2 * fr) * G::S_G + i] = gc;
-        gsm[(2 * fr + 1) * G::S_G + i] = gr;
-      }
-    }
-    for (int i = tid; i < G::OY * G::RIW; i += G::NT) {
-      const int oy = i / G::RIW, cc = i % G::RIW;
-      const int nyo = ny0 + oy / M;
-      float w5[5];
-#pragma unroll
-      for (int k = 0; k < 5; ++k) w5[k] = rw[oy * 5 + k];
-      const int off = (nyo - 2 - y_start) * G::BW + (nx0 - 2 + cc - x_start);
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        const float* col = tin[fr] + off;
-        float s = 0.f;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) s = fmaf(w5[k], col[k * G::BW], s);
-        ri[fr * G::S_RI + i] = s;
-      }
-    }
-    __syncthreads();
-    if (use_tma) {
-      // this set's input buffers are free: fetch the frames two passes ahead
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        const int fn = fa + 2 * FP + fr;
-        const int k = set * FP + fr;
-        if (fn < f1) {
-          if (tid == 0) {
-            if (fr == 0) fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bar[k], kTileBytes);
-            tma_load_3d(inb + k * G::S_INB, tmap, &bar[k], x_start, y_start, fn);
-          }
-          pend |= 1u << k;
+  if (producer) {
+    // ======================= producer warpgroup =============================
+    constexpr unsigned kTileBytes = unsigned(G::BH * G::BW * 4);
+    const bool use_tma = p.tmap >= 0;
+    const CUtensorMap* tmap = use_tma ? &maps.m[p.tmap] : nullptr;
+    const bool leader = prod.ptid == 0;
+    if (use_tma && leader) {
+      // input buffer k = set * FP + fr holds frame f0 + k for the first two sets
+      fence_proxy_async_smem();
+      for (int k = 0; k < 2 * FP; ++k) {
+        if (f0 + k < f1) {
+          mbar_arrive_expect_tx(&tbar[k], kTileBytes);
+          tma_load_3d(prod.inb + k * G::S_INB, tmap, &tbar[k], u.x_start, u.y_start, f0 + k);
+          tpend |= 1u << k;
         }
       }
     }
-
-    // ---- phase 2: gradient column pass onto half-grid columns --------------
-    for (int i = tid; i < G::NRY * G::HG_C; i += G::NT) {
-      const int rl = i / G::HG_C, kxl = i % G::HG_C;
-      const int kx = kb_x + kxl;
-      float vc[FP], vr[FP];
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) vc[fr] = vr[fr] = 0.f;
-      if (kx >= 1 && kx <= kmax_x) {
-        if (kx >= twoW) {
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX;
-            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX;
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-              const int cl = p.cx_base + t - CX0;
-              vc[fr] = fmaf(p.cx[t], g0[cl], vc[fr]);
-              vr[fr] = fmaf(p.cx[t], g1[cl], vr[fr]);
-            }
-          }
-        } else if (kx & 1) {
-          const int cl = ((kx - 1) >> 1) - CX0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            vc[fr] = gsm[(2 * fr) * G::S_G + rl * G::NCX + cl];
-            vr[fr] = gsm[(2 * fr + 1) * G::S_G + rl * G::NCX + cl];
-          }
-        } else {
-          const int cl = (kx >> 1) - 2 - CX0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX + cl;
-            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX + cl;
-            float c = -0.0625f * g0[0], r = -0.0625f * g1[0];
-            c = fmaf(0.5625f, g0[1], c);
-            r = fmaf(0.5625f, g1[1], r);
-            c = fmaf(0.5625f, g0[2], c);
-            r = fmaf(0.5625f, g1[2], r);
-            vc[fr] = fmaf(-0.0625f, g0[3], c);
-            vr[fr] = fmaf(-0.0625f, g1[3], r);
-          }
-        }
-      }
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        t1[(2 * fr) * G::S_T1 + i] = vc[fr];
-        t1[(2 * fr + 1) * G::S_T1 + i] = vr[fr];
-      }
-    }
-    __syncthreads();
-
-    // ---- phase 3: gradient row pass, normalise -> half-grid tile ----------
-    for (int i = tid; i < G::HG_R * G::HG_C; i += G::NT) {
-      const int kyl = i / G::HG_C, kxl = i % G::HG_C;
-      const int ky = kb_y + kyl, kx = kb_x + kxl;
-      float nxv[FP], nyv[FP];
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) nxv[fr] = nyv[fr] = 0.f;
-      if (ky >= 1 && ky <= kmax_y && kx >= 1 && kx <= kmax_x) {
-        float gx[FP], gy[FP];
-        if (ky >= twoH) {
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* c0 = t1 + (2 * fr) * G::S_T1 + kxl;
-            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + kxl;
-            gx[fr] = gy[fr] = 0.f;
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-              const int rl = p.cy_base + t - RY0;
-              gx[fr] = fmaf(p.cy[t], c0[rl * G::HG_C], gx[fr]);
-              gy[fr] = fmaf(p.cy[t], c1[rl * G::HG_C], gy[fr]);
-            }
-          }
-        } else if (ky & 1) {
-          const int rl = ((ky - 1) >> 1) - RY0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            gx[fr] = t1[(2 * fr) * G::S_T1 + rl * G::HG_C + kxl];
-            gy[fr] = t1[(2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl];
-          }
-        } else {
-          const int rl = (ky >> 1) - 2 - RY0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* c0 = t1 + (2 * fr) * G::S_T1 + rl * G::HG_C + kxl;
-            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl;
-            float x = -0.0625f * c0[0], y = -0.0625f * c1[0];
-            x = fmaf(0.5625f, c0[G::HG_C], x);
-            y = fmaf(0.5625f, c1[G::HG_C], y);
-            x = fmaf(0.5625f, c0[2 * G::HG_C], x);
-            y = fmaf(0.5625f, c1[2 * G::HG_C], y);
-            gx[fr] = fmaf(-0.0625f, c0[3 * G::HG_C], x);
-            gy[fr] = fmaf(-0.0625f, c1[3 * G::HG_C], y);
-          }
-        }
-#pragma unroll
-        for (int fr = 0; fr < FP; ++fr) {
-          const float m2 = fmaf(gx[fr], gx[fr], gy[fr] * gy[fr]);
-          if (m2 > 0.f) {
-            const float inv = rsqrtf(m2);
-            nxv[fr] = gx[fr] * inv;
-            nyv[fr] = gy[fr] * inv;
-          }
-        }
-      }
-      const int o = (kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1);
-      if constexpr (FP == 2)
-        reinterpret_cast<float4*>(hgf)[o] = make_float4(nxv[0], nxv[1], nyv[0], nyv[1]);
-      else
-        reinterpret_cast<float2*>(hgf)[o] = make_float2(nxv[0], nyv[0]);
-    }
-    __syncthreads();
-
-    // ---- phase 4: RGC for this thread's M outputs --------------------------
-    // contribution of sample (phase, offset): (dp < 0) ? w - |u| : 0 with
-    // dp = n.(a, b) and u = n x (a, b) (n the unit gradient)
-    float acc[FP][M];
-#pragma unroll
-    for (int fr = 0; fr < FP; ++fr)
-#pragma unroll
-      for (int px = 0; px < M; ++px) acc[fr][px] = 0.f;
-    if constexpr (FP == 1) {
-      const float2* hg = reinterpret_cast<const float2*>(hgf);
-#pragma unroll
-      for (int jj = 0; jj < G::W2; ++jj) {
-        const int kyl = 2 * ty + cpy + jj;
-        const float2* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
-        const float2* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
-        float2 sv[G::NQ];
-#pragma unroll
-        for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
-        const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * G::TBLK;
-#pragma unroll
-        for (int s4 = 0; s4 < G::NS4; ++s4) {
-          const float4 A = tb[s4];
-          const float4 B = tb[G::NS4 + s4];
-          const float4 Wv = tb[2 * G::NS4 + s4];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int sidx = s4 * 4 + e;
-            if (sidx < G::NS) {
-              const int px = sidx / G::W2;
-              const int ii = sidx % G::W2;
-              const int cpx = (2 * px + 1) / M;
-              const float2 gv = sv[cpx + ii];
-              const float a = f4c(A, e), bb = f4c(B, e), w = f4c(Wv, e);
-              const float dp = fmaf(gv.x, a, gv.y * bb);
-              const float u = fmaf(gv.y, a, -(gv.x * bb));
-              const float v = w - fabsf(u);
-              acc[0][px] = (dp < 0.f) ? acc[0][px] + v : acc[0][px];
-            }
-          }
-        }
-      }
-    } else {
-      // frame pair in one register pair: gx = (gx0, gx1), gy = (gy0, gy1)
-      const float4* hg = reinterpret_cast<const float4*>(hgf);
-      // every FMA-pipe operation is packed (both frames in one instruction):
-      //   v = w + (-|u|), acc += [dp < 0] * v
-      // measured 6 % faster than scalar v and predicated scalar adds
-      float2 acc2[M];
-#pragma unroll
-      for (int px = 0; px < M; ++px) acc2[px] = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int jj = 0; jj < G::W2; ++jj) {
-        const int kyl = 2 * ty + cpy + jj;
-        const float4* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
-        const float4* r1 = hg + (kyl * 2 + 1) * G::HGP + lane;
-        float4 sv[G::NQ];
-#pragma unroll
-        for (int q = 0; q < G::NQ; ++q) sv[q] = (q & 1) ? r1[q >> 1] : r0[q >> 1];
-        const float4* tb = tb4 + (size_t)(py * G::W2 + jj) * G::TBLK;
-#pragma unroll
-        for (int sidx = 0; sidx < G::NS; ++sidx) {
-          const int px = sidx / G::W2;
-          const int ii = sidx % G::W2;
-          const int cpx = (2 * px + 1) / M;
-          const float4 g = sv[cpx + ii];
-          const float2 gx = make_float2(g.x, g.y), gy = make_float2(g.z, g.w);
-          const float4 T = tb[sidx];
-          const float2 a = make_float2(T.x, T.x), b = make_float2(T.y, T.y);
-          const float2 nb = make_float2(T.z, T.z);
-          const float w = T.w;
-          const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
-          const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
-          const float2 nu = make_float2(__int_as_float(__float_as_int(u.x) | 0x80000000),
-                                        __int_as_float(__float_as_int(u.y) | 0x80000000));
-          const float2 v = __fadd2_rn(make_float2(w, w), nu);
-          const float2 msk = make_float2(dp.x < 0.f ? 1.f : 0.f, dp.y < 0.f ? 1.f : 0.f);
-          acc2[px] = __ffma2_rn(msk, v, acc2[px]);
-        }
-      }
-#pragma unroll
-      for (int px = 0; px < M; ++px) {
-        acc[0][px] = acc2[px].x;
-        acc[FP - 1][px] = acc2[px].y;
-      }
-    }
-
-    // ---- epilogue: normalise, ^sensitivity, intensity, margin, temporal ----
-    // magnified intensity of this thread's outputs: column pass of the
-    // Catmull-Rom interpolation from the row-pass values (5 taps per output)
-    float rv[FP][5];
-    if (p.iw) {
+    for (int j = 0; j < npass; ++j) {
+      const unsigned g = gp + j;
+      const int s = g & 1;
+      const unsigned use = g >> 1;
+      const int fa = f0 + j * FP;
+      const int set = j & 1;
+      const int nf = min(FP, f1 - fa);
+      const float* tin[FP];
 #pragma unroll
       for (int fr = 0; fr < FP; ++fr)
+        tin[fr] = prod.inb + (set * FP + (fr < nf ? fr : 0)) * G::S_INB;
+      // slot s is free once the consumers released its previous use
+      bool ok = use == 0 || mbar_wait_or_abort(&empty[s], (use - 1) & 1u, &s_abort);
+      if (ok && use_tma) {
 #pragma unroll
-        for (int k = 0; k < 5; ++k) rv[fr][k] = ri[fr * G::S_RI + (ty * M + py) * G::RIW + lane + k];
-    }
-    const bool first = (fa == f0);
-#pragma unroll
-    for (int px = 0; px < M; ++px) {
-      const float twv = tw[px * G::NT + tid];
-      const bool zero = (omask & (1u << px)) != 0;
-      float base[FP], ival[FP];
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        base[fr] = acc[fr][px] * twv;
-        base[fr] = (base[fr] < 0.f) ? 0.f : base[fr];
+        for (int fr = 0; fr < FP; ++fr) {
+          const int k = set * FP + fr;
+          if (fr < nf && ok) {
+            ok = mbar_wait_or_abort(&tbar[k], (tphase >> k) & 1u, &s_abort);
+            if (ok) {
+              tphase ^= 1u << k;
+              tpend &= ~(1u << k);
+            }
+          }
+        }
+      } else if (ok) {
+        for (int fr = 0; fr < nf; ++fr) {
+          const float* src = p.in + (size_t)(fa + fr) * u.H * u.W;
+          float* dst = prod.inb + (set * FP + fr) * G::S_INB;
+          for (int i = prod.ptid; i < G::BH * G::BW; i += G::NP) {
+            const int r = u.y_start + i / G::BW;
+            const int c = u.x_start + i % G::BW;
+            dst[i] = (r >= 0 && r < u.H && c >= 0 && c < u.W) ? __ldg(src + (size_t)r * u.W + c)
+                                                               : 0.f;
+          }
+        }
+        mbar_arrive(pbar);
+        ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort);
+        pphase ^= 1u;
       }
+      if (!ok) {
+        *(volatile int*)&s_abort = 1;
+        break;
+      }
+      prod.roberts_and_rows(p, u, tin, s);
+      mbar_arrive(pbar);
+      ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort);
+      pphase ^= 1u;
+      if (!ok) {
+        *(volatile int*)&s_abort = 1;
+        break;
+      }
+      if (use_tma && leader) {
+        // this set's input buffers are free: fetch the frames two passes ahead
+        fence_proxy_async_smem();
 #pragma unroll
-      for (int fr = 0; fr < FP; ++fr) ival[fr] = 1.f;
-      if (p.iw) {
-        float w5[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) w5[k] = cw[(lane * M + px) * 5 + k];
-        if constexpr (FP == 2) {
-          float2 s2 = make_float2(0.f, 0.f);
-#pragma unroll
-          for (int k = 0; k < 5; ++k)
-            s2 = __ffma2_rn(make_float2(w5[k], w5[k]), make_float2(rv[0][k], rv[FP - 1][k]), s2);
-          ival[0] = s2.x;
-          ival[FP - 1] = s2.y;
-        } else {
-          float s1 = 0.f;
-#pragma unroll
-          for (int k = 0; k < 5; ++k) s1 = fmaf(w5[k], rv[0][k], s1);
-          ival[0] = s1;
+        for (int fr = 0; fr < FP; ++fr) {
+          const int fn = fa + 2 * FP + fr;
+          const int k = set * FP + fr;
+          if (fn < f1) {
+            mbar_arrive_expect_tx(&tbar[k], kTileBytes);
+            tma_load_3d(prod.inb + k * G::S_INB, tmap, &tbar[k], u.x_start, u.y_start, fn);
+            tpend |= 1u << k;
+          }
         }
       }
-      if (MODE == kModeSum) {
-        for (int k = 0; k < p.n_sens; ++k) {
-          float2* ks = reinterpret_cast<float2*>(tk) + (k * M + px) * G::NT + tid;
-          float kv = 0.f, sv = 0.f;
+      prod.column_pass(p, u);
+      mbar_arrive(pbar);
+      ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort);
+      pphase ^= 1u;
+      if (!ok) {
+        *(volatile int*)&s_abort = 1;
+        break;
+      }
+      prod.row_pass(p, u, s);
+      mbar_arrive(&full[s]);
+    }
+  } else {
+    // ======================= consumers ======================================
+    const size_t plane = (size_t)p.rowsM * p.colsM;
+    for (int j = 0; j < npass; ++j) {
+      const unsigned g = gp + j;
+      const int s = g & 1;
+      const unsigned use = g >> 1;
+      const int fa = f0 + j * FP;
+      const int nf = min(FP, f1 - fa);
+      if (!mbar_wait_or_abort(&full[s], use & 1u, &s_abort)) {
+        *(volatile int*)&s_abort = 1;
+        break;
+      }
+      float acc[FP][M];
+      rgc_core<M, J, TY, FP>(sm + G::O_HG + s * G::S_HG, tb4, ty, py, lane, acc);
+
+      // ---- normalise, ^sensitivity, intensity, margin, temporal ------------
+      // magnified intensity of this thread's outputs: column pass of the
+      // Catmull-Rom interpolation from the row-pass values (5 taps per output)
+      const float* ri = sm + G::O_RI + s * FP * G::S_RI;
+      float rv[FP][5];
+      if (p.iw) {
+#pragma unroll
+        for (int fr = 0; fr < FP; ++fr)
+#pragma unroll
+          for (int k = 0; k < 5; ++k) rv[fr][k] = ri[fr * G::S_RI + (ty * M + py) * G::RIW + lane + k];
+      }
+      mbar_arrive(&empty[s]);  // slot s fully read
+      const bool first = (fa == f0);
+#pragma unroll
+      for (int px = 0; px < M; ++px) {
+        const float twv = tw[px * G::NTC + tid];
+        const bool zero = (omask & (1u << px)) != 0;
+        float base[FP], ival[FP];
+#pragma unroll
+        for (int fr = 0; fr < FP; ++fr) {
+          base[fr] = acc[fr][px] * twv;
+          base[fr] = (base[fr] < 0.f) ? 0.f : base[fr];
+          ival[fr] = 1.f;
+        }
+        if (p.iw) {
+          float w5[5];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) w5[k] = cw[(lane * M + px) * 5 + k];
+          if constexpr (FP == 2) {
+            float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+              s2 = __ffma2_rn(make_float2(w5[k], w5[k]), make_float2(rv[0][k], rv[FP - 1][k]), s2);
+            ival[0] = s2.x;
+            ival[FP - 1] = s2.y;
+          } else {
+            float s1 = 0.f;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) s1 = fmaf(w5[k], rv[0][k], s1);
+            ival[0] = s1;
+          }
+        }
+        if (MODE == kModeSum) {
+          for (int k = 0; k < p.n_sens; ++k) {
+            float2* ks = reinterpret_cast<float2*>(tk) + (k * M + px) * G::NTC + tid;
+            float kv = 0.f, sv = 0.f;
+            if (!first) {
+              const float2 t = *ks;
+              kv = t.x;
+              sv = t.y;
+            }
+#pragma unroll
+            for (int fr = 0; fr < FP; ++fr) {
+              if (fr < nf) {
+                float r = apply_sens(base[fr], p.sens_mode_k[k], p.sens_int_k[k], p.sens_k[k]);
+                r = zero ? 0.f : r * ival[fr];
+                if (first && fr == 0) {
+                  kv = r;
+                  sv = 0.f;
+                } else {
+                  sv += r - kv;
+                }
+              }
+            }
+            *ks = make_float2(kv, sv);
+          }
+        } else if (MODE == kModeStack) {
+#pragma unroll
+          for (int fr = 0; fr < FP; ++fr) {
+            if (fr < nf) {
+              float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
+              r = zero ? 0.f : r * ival[fr];
+              if (!(omask >> 31))
+                p.out[(size_t)(fa + fr) * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
+            }
+          }
+        } else {
+          float4* st = reinterpret_cast<float4*>(tk) + px * G::NTC + tid;
+          float* stl = tk + 4 * M * G::NTC + px * G::NTC + tid;
+          float K = 0.f, S = 0.f, Q = 0.f, P = 0.f, L = 0.f;
           if (!first) {
-            const float2 t = *ks;
-            kv = t.x;
-            sv = t.y;
+            const float4 t = *st;
+            K = t.x;
+            S = t.y;
+            Q = t.z;
+            P = t.w;
+            L = *stl;
           }
 #pragma unroll
           for (int fr = 0; fr < FP; ++fr) {
             if (fr < nf) {
-              float r = apply_sens(base[fr], p.sens_mode_k[k], p.sens_int_k[k], p.sens_k[k]);
+              float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
               r = zero ? 0.f : r * ival[fr];
               if (first && fr == 0) {
-                kv = r;
-                sv = 0.f;
+                K = r;
               } else {
-                sv += r - kv;
+                const float y = r - K;
+                S += y;
+                Q = fmaf(y, y, Q);
+                P = fmaf(L, y, P);
+                L = y;
               }
             }
           }
-          *ks = make_float2(kv, sv);
+          *st = make_float4(K, S, Q, P);
+          *stl = L;
         }
-      } else if (MODE == kModeStack) {
-#pragma unroll
-        for (int fr = 0; fr < FP; ++fr) {
-          if (fr < nf) {
-            float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
-            r = zero ? 0.f : r * ival[fr];
-            if (!(omask >> 31))
-              p.out[(size_t)(fa + fr) * plane + (size_t)yM * p.colsM + (size_t)nx * M + px] = r;
-          }
-        }
-      } else {
-        float4* st = reinterpret_cast<float4*>(tk) + px * G::NT + tid;
-        float* stl = tk + 4 * M * G::NT + px * G::NT + tid;
-        float K = 0.f, S = 0.f, Q = 0.f, P = 0.f, L = 0.f;
-        if (!first) {
-          const float4 t = *st;
-          K = t.x;
-          S = t.y;
-          Q = t.z;
-          P = t.w;
-          L = *stl;
-        }
-#pragma unroll
-        for (int fr = 0; fr < FP; ++fr) {
-          if (fr < nf) {
-            float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
-            r = zero ? 0.f : r * ival[fr];
-            if (first && fr == 0) {
-              K = r;
-            } else {
-              const float y = r - K;
-              S += y;
-              Q = fmaf(y, y, Q);
-              P = fmaf(L, y, P);
-              L = y;
-            }
-          }
-        }
-        *st = make_float4(K, S, Q, P);
-        *stl = L;
       }
     }
   }
-
-  if (aborted) {
-    // a TMA tile never arrived: wait (bounded) for the copies still in flight,
-    // then leave without writing
-    if (tid == 0) {
-      for (int k = 0; k < 2 * FP; ++k)
-        if (pend & (1u << k)) (void)mbar_wait_bounded(&bar[k], (phase >> k) & 1u);
-    }
-    return;
-  }
-
-  if (MODE != kModeStack && !(omask >> 31)) {
+  if (!producer && s_abort == 0 && MODE != kModeStack && !(omask >> 31)) {
+    const size_t plane = (size_t)p.rowsM * p.colsM;
     float* rec = p.out + (size_t)(tp * p.chunks + chunk) * p.F * plane +
                  (size_t)yM * p.colsM + (size_t)nx * M;
     if (MODE == kModeSum) {
       for (int k = 0; k < p.n_sens; ++k) {
 #pragma unroll
         for (int px = 0; px < M; ++px) {
-          const float2 t = reinterpret_cast<const float2*>(tk)[(k * M + px) * G::NT + tid];
+          const float2 t = reinterpret_cast<const float2*>(tk)[(k * M + px) * G::NTC + tid];
           rec[(2 * k) * plane + px] = t.x;
           rec[(2 * k + 1) * plane + px] = t.y;
         }
@@ -811,17 +903,28 @@ __global__ void __launch_bounds__(32 * TY * M, (32 * TY * M <= 384) ? 2 : 1)
     } else {
 #pragma unroll
       for (int px = 0; px < M; ++px) {
-        const float4 t = reinterpret_cast<const float4*>(tk)[px * G::NT + tid];
+        const float4 t = reinterpret_cast<const float4*>(tk)[px * G::NTC + tid];
         rec[px] = t.x;
         rec[plane + px] = t.y;
         rec[2 * plane + px] = t.z;
         rec[3 * plane + px] = t.w;
-        rec[4 * plane + px] = tk[4 * M * G::NT + px * G::NT + tid];
+        rec[4 * plane + px] = tk[4 * M * G::NTC + px * G::NTC + tid];
       }
     }
   }
   }  // chunk < nch
   __syncthreads();  // the unit's shared state is free for the next unit
+  if (s_abort) {
+    // a wait ran out: the producer leader waits (bounded) for its TMA copies
+    // still in flight, then every thread leaves without writing more
+    if (producer && prod.ptid == 0 && p.status) atomicOr(p.status, kDevTmaTimeout);
+    if (producer && prod.ptid == 0) {
+      for (int k = 0; k < 2 * FP; ++k)
+        if (tpend & (1u << k)) (void)mbar_wait_bounded(&tbar[k], (tphase >> k) & 1u);
+    }
+    return;
+  }
+  gp += npass;
   }  // unit loop
 }
 
@@ -882,8 +985,8 @@ struct FusedGeometry {
 
 template <int M, int J>
 FusedGeometry fused_geometry() {
-  using G = Geo<M, J, TileRows<M>::TY, 1>;
-  return FusedGeometry{TileRows<M>::TY, G::IX, G::IY, G::BW, G::BH};
+  using G = Geo<M, J, EsrrfTile<M>::TY, 1>;
+  return FusedGeometry{EsrrfTile<M>::TY, G::IX, G::IY, G::BW, G::BH};
 }
 
 }  // namespace nx
