@@ -38,6 +38,9 @@ CFG = dict(T=500, H=512, W=512, emitters=400, m=5, radius=1.5, sensitivity=2.0,
            correlations=("VAR", "TAC2"), fpt=100, mpc=True, seed=1)
 # profiling case: same kernel and frame size, 160 frames (168 MB input, still > L2)
 SMALL = dict(T=160, fpt=80)
+# DRAM bytes of one fused launch, dram__bytes_read.sum + dram__bytes_write.sum from a
+# 1-pass ncu capture of that launch (large: the full 500-frame launch; small: 160 frames)
+TRAFFIC_BYTES = {"large": 532740352 + 608213504, "small": 169642496 + 209450752}
 METRIC = "eSRRF input Mpx*frames/s"
 REF_SAMPLE_FRAMES = 4
 
@@ -384,7 +387,9 @@ def run_gpu_arm(args):
                 "h2d_bytes_per_step": int(stack_np.nbytes), "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": args.steps * (1 + n_tp + 2),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": TRAFFIC_BYTES.get(args.workload),
+                     "traffic_unit": "bytes per launch (ncu DRAM read + write)",
                      "kernel": f"esrrf_fused_kernel<m={m},J={int(2 * R)},FULL>",
                      "kernel_ms": kern_ms,
                      "flops_per_launch": flops, "samples_per_output": S,
