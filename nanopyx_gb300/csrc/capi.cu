@@ -295,7 +295,11 @@ static int launch_fused_mode(const nx_esrrf_plan* p, int mode, const float* d_in
   ut.n_items = 1;
   ut.ns_cap = 1;
   ut.total_units = (int)units;
-  cudaError_t e = p->fused->launch[mode](ut, pack, ut.total_units, s);
+  // persistent grid: the resident CTAs stride over the units (setup and the
+  // phase-table copy once per CTA instead of once per unit)
+  const long long resident = (long long)p->fused->occupancy[mode](1) * device_sms();
+  const int grid = (int)std::min<long long>(units, std::max<long long>(1, resident));
+  cudaError_t e = p->fused->launch[mode](ut, pack, grid, s);
   if (e != cudaSuccess) return cuda_status(e, "fused eSRRF launch");
   return NX_OK;
 }
