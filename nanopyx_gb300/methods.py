@@ -104,14 +104,17 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
                 names, doIntensityWeighting, macro_pixel_correction) -> np.ndarray:
     """eSRRF with host buffers, copies overlapped with compute.
 
-    The stack is uploaded in segments on a copy stream (a timepoint, or a
-    quarter of it when there are fewer than three timepoints); each segment is
-    folded into its timepoint's device-resident accumulator on the compute
-    stream while the next one uploads, and each finished timepoint is copied
-    back while the next computes.  Same arithmetic as ``esrrf_device``.
+    The stack is uploaded in segments (a timepoint, or a quarter of it when
+    there are fewer than three timepoints): host threads copy a segment into
+    one of two pinned buffers, a copy stream moves it to the device, and the
+    compute stream folds it into its timepoint's device-resident accumulator
+    while the next segment is staged.  Each finished timepoint goes back the
+    same way (device -> pinned on the copy stream, pinned -> result by the host
+    threads) while the next computes.  Same arithmetic as ``esrrf_device``.
     Returns (n_corr, n_timepoints, H*m, W*m) float32.
     """
     from ._device import require_cuda
+    from ._hostio import par_copy, pinned
 
     dev = require_cuda()
     T, H, W = arr.shape
@@ -140,38 +143,63 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
            for _ in range(2)]
     outs = [torch.empty((len(order), H * m, W * m), dtype=torch.float32, device=dev)
             for _ in range(2)]
+    seg_dev = [torch.empty((max_seg, H, W), dtype=torch.float32, device=dev) for _ in range(2)]
+    seg_pin = [pinned((max_seg, H, W)) for _ in range(2)]
+    out_pin = [pinned((len(order), H * m, W * m)) for _ in range(2)]
+    seg_free = [None, None]  # event: the H2D copy out of seg_pin[i] has finished
+    seg_used = [None, None]  # event: the push reading seg_dev[i] has finished
     res = np.empty((len(names), n_tp, H * m, W * m), dtype=np.float32)
     done = [None, None]
+    back = [None, None]
 
-    def drain(tp):
+    def fetch(tp):
+        # device -> pinned on the copy stream once timepoint tp is finalised
         k = tp & 1
         cp.wait_event(done[k])
         with torch.cuda.stream(cp):
-            host = outs[k].cpu()
-        res[:, tp] = host.numpy()[sel]
+            out_pin[k].copy_(outs[k], non_blocking=True)
+            back[k] = cp.record_event()
+
+    def drain(tp):
+        k = tp & 1
+        back[k].synchronize()
+        src = out_pin[k].numpy()
+        for i, si in enumerate(sel):
+            par_copy(res[i, tp], src[si])
 
     pending = None
+    iseg = 0
     for tp in range(n_tp):
         a0, a1 = tp * fpt, min(T, (tp + 1) * fpt)
         k = tp & 1
         before = 0
         for sa in range(a0, a1, seg_len):
             sb = min(a1, sa + seg_len)
+            j = iseg & 1
+            iseg += 1
+            if seg_free[j] is not None:
+                seg_free[j].synchronize()
+            par_copy(seg_pin[j].numpy()[: sb - sa], arr[sa:sb])
             with torch.cuda.stream(cp):
-                seg = torch.from_numpy(arr[sa:sb]).to(dev, non_blocking=True)
-            comp.wait_stream(cp)
-            seg.record_stream(comp)
-            N.check(L.nx_esrrf_accum_push(plan.handle, seg.data_ptr(), sb - sa, before,
+                # seg_dev[j] is free once the push two segments ago has run
+                if seg_used[j] is not None:
+                    cp.wait_event(seg_used[j])
+                seg_dev[j][: sb - sa].copy_(seg_pin[j][: sb - sa], non_blocking=True)
+                seg_free[j] = cp.record_event()
+            comp.wait_event(seg_free[j])
+            N.check(L.nx_esrrf_accum_push(plan.handle, seg_dev[j].data_ptr(), sb - sa, before,
                                           acc[k].data_ptr(), ws_push.data_ptr(), ws_push.numel(),
                                           comp.cuda_stream), "eSRRF push")
+            seg_used[j] = comp.record_event()
             before += sb - sa
         if pending is not None:
-            drain(pending)  # outs[pending & 1] is free again after this
+            drain(pending)  # outs / out_pin of pending & 1 are free again after this
         N.check(L.nx_esrrf_accum_finalize(plan.handle, acc[k].data_ptr(), before, mask,
                                           1 if macro_pixel_correction else 0,
                                           outs[k].data_ptr(), ws_fin.data_ptr(),
                                           ws_fin.numel(), comp.cuda_stream), "eSRRF finalize")
         done[k] = comp.record_event()
+        fetch(tp)
         pending = tp
     drain(pending)
     N.check(L.nx_workspace_status(ws_push.data_ptr(), comp.cuda_stream), "eSRRF")
