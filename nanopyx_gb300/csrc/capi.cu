@@ -214,16 +214,33 @@ static int check_plan(const nx_esrrf_plan* p) {
 }
 
 // chunking of each timepoint's frames across CTAs (deterministic in its inputs)
+// Frame chunks per timepoint of a single-stack launch.  The resident CTAs
+// stride over (tile, timepoint, chunk) units, so a CTA runs about
+// ceil(units / resident) units, each costing its frame passes plus a start-up
+// of ~0.65 pass (the unit's first pass is not overlapped with the producer
+// warps' preparation).  The chunk count with the smallest estimate wins: few
+// chunks for large stacks, enough to fill every SM for small ones.
 static int plan_chunks(const nx_esrrf_plan* p, int T, int fpt, int n_tp) {
   if (!p->fused) return 1;
   const int TY = p->fused->geo.TY;
   const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + TY - 1) / TY);
   const int min_nf = std::min(fpt, T - (n_tp - 1) * fpt);
-  const long long target = 3LL * device_sms();
-  long long c = (target + tiles * n_tp - 1) / (tiles * n_tp);
-  c = std::min<long long>(c, std::max(1, min_nf / 4));
-  c = std::max<long long>(1, std::min<long long>(c, min_nf));
-  return (int)c;
+  const long long resident =
+      (long long)std::max(1, p->fused->occupancy[kModeFull](1)) * device_sms();
+  int best = 1;
+  double best_cost = 1e300;
+  const int cmax = std::max(1, std::min(min_nf / 4, 64));  // >= 4 frames per chunk
+  for (int c = 1; c <= cmax; ++c) {
+    const long long units = tiles * n_tp * c;
+    const double per_cta = (double)((units + resident - 1) / resident);
+    const double passes = std::ceil((double)fpt / c / 2.0);
+    const double cost = per_cta * (passes + 0.65);
+    if (cost < best_cost * 0.999) {
+      best_cost = cost;
+      best = c;
+    }
+  }
+  return best;
 }
 
 static size_t align256(size_t b) { return (b + 255) / 256 * 256; }

@@ -133,11 +133,22 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
     L = N.lib()
     plan = get_plan(H, W, m, radius, sensitivity, doIntensityWeighting)
     comp = torch.cuda.current_stream(dev)
-    cp = torch.cuda.Stream(dev)
+    cp = torch.cuda.Stream(dev)   # host -> device
+    cpo = torch.cuda.Stream(dev)  # device -> host (never queues behind an upload)
     nseg = 1 if n_tp >= 3 else min(4, fpt)
     seg_len = -(-fpt // nseg)
     max_seg = min(seg_len, T)
-    ws_push = workspace(L.nx_esrrf_push_workspace_bytes(plan.handle, max_seg), dev)
+    # the first timepoint goes up as a short head segment and the rest, so the
+    # device starts after ~1/5 of a timepoint has been staged
+    head = fpt // 5 if nseg == 1 and fpt >= 10 else seg_len
+    segs = []  # per timepoint: segment bounds [(sa, sb), ...]
+    for tp in range(n_tp):
+        a0, a1 = tp * fpt, min(T, (tp + 1) * fpt)
+        cuts = [a0 + head] if tp == 0 and head < seg_len else []
+        cuts += list(range(a0 + seg_len, a1, seg_len)) + [a1]
+        segs.append(list(zip([a0] + cuts[:-1], cuts)))
+    ws_push = workspace(max(L.nx_esrrf_push_workspace_bytes(plan.handle, n)
+                            for n in {sb - sa for tsegs in segs for sa, sb in tsegs}), dev)
     ws_fin = workspace(256 + L.nx_macro_pixel_workspace_bytes(3, m), dev)
     acc = [torch.empty(L.nx_esrrf_accum_bytes(plan.handle), dtype=torch.uint8, device=dev)
            for _ in range(2)]
@@ -153,12 +164,12 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
     back = [None, None]
 
     def fetch(tp):
-        # device -> pinned on the copy stream once timepoint tp is finalised
+        # device -> pinned on the download stream once timepoint tp is finalised
         k = tp & 1
-        cp.wait_event(done[k])
-        with torch.cuda.stream(cp):
+        cpo.wait_event(done[k])
+        with torch.cuda.stream(cpo):
             out_pin[k].copy_(outs[k], non_blocking=True)
-            back[k] = cp.record_event()
+            back[k] = cpo.record_event()
 
     def drain(tp):
         k = tp & 1
@@ -170,11 +181,9 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
     pending = None
     iseg = 0
     for tp in range(n_tp):
-        a0, a1 = tp * fpt, min(T, (tp + 1) * fpt)
         k = tp & 1
         before = 0
-        for sa in range(a0, a1, seg_len):
-            sb = min(a1, sa + seg_len)
+        for sa, sb in segs[tp]:
             j = iseg & 1
             iseg += 1
             if seg_free[j] is not None:
