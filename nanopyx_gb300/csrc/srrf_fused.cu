@@ -43,7 +43,9 @@ struct SrrfTile {
   static constexpr int O_RT = O_CW + al(OX * 5);        // ring row taps [OY][12][8]
   // ring col taps: float4 halves [ring][px][2][lane] (lane-contiguous, conflict-free)
   static constexpr int O_CT = O_RT + al(OY * kRing * 8);
-  static constexpr int FLOATS = O_CT + al(OX * kRing * 8);
+  // per-warp row pass of the gradient interpolation: [warp][ring][IW] float2
+  static constexpr int O_RB = O_CT + al(OX * kRing * 8);
+  static constexpr int FLOATS = O_RB + (NT / 32) * kRing * IW * 2;
   static constexpr size_t SMEM = size_t(FLOATS) * 4;
 };
 
@@ -87,6 +89,7 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
   float* cw = sm + G::O_CW;
   float* rt = sm + G::O_RT;
   float* ct = sm + G::O_CT;
+  float2* rb = reinterpret_cast<float2*>(sm + G::O_RB) + (threadIdx.x >> 5) * kRing * G::IW;
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -199,6 +202,29 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
       }
       __syncthreads();
     }
+    // row pass of the ring interpolation: the ring points of this warp's output
+    // row share their tap rows and weights, so each (ring point, tile column)
+    // sum over the 4 tap rows is formed once per warp (same fma order as the
+    // 16-tap form: rows first, then columns)
+    for (int idx = lane; idx < kRing * G::IW; idx += 32) {
+      const int s = idx / G::IW, c = idx - s * G::IW;
+      const float4 rA = *reinterpret_cast<const float4*>(rrow + s * 8);
+      const float4 rB = *reinterpret_cast<const float4*>(rrow + s * 8 + 4);
+      float2 v = make_float2(0.f, 0.f);
+      if (rB.z != 0.f) {
+        const int r0 = __float_as_int(rA.x) - y_start;
+        const float wr[4] = {rA.y, rA.z, rA.w, rB.x};
+        const float2* gp = grad + r0 * G::IW + c;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const float2 g = gp[t * G::IW];
+          v.x = fmaf(g.x, wr[t], v.x);
+          v.y = fmaf(g.y, wr[t], v.y);
+        }
+      }
+      rb[idx] = v;
+    }
+    __syncwarp();
     // radiality of this thread's M outputs
 #pragma unroll 1
     for (int px = 0; px < M; ++px) {
@@ -207,32 +233,22 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
       if (row_ok && nx < w && i >= lo_i && i < hi_i) {
         const float4* crow = reinterpret_cast<const float4*>(ct) + (px * 2) * 32 + lane;
         float div = 0.f;
-#pragma unroll 2
+#pragma unroll 4
         for (int s = 0; s < kRing; ++s) {
-          const float* re = rrow + s * 8;
-          const float4 rA = *reinterpret_cast<const float4*>(re);
-          const float4 rB = *reinterpret_cast<const float4*>(re + 4);
+          const float4 rB = *reinterpret_cast<const float4*>(rrow + s * 8 + 4);
           const float4 cA = crow[(s * M * 2) * 32];
           const float4 cB = crow[(s * M * 2 + 1) * 32];
           float dk = 0.f;
           float vgx = 0.f, vgy = 0.f;
           if (rB.z != 0.f && cB.z != 0.f) {
-            const int r0 = __float_as_int(rA.x) - y_start;
             const int c0 = __float_as_int(cA.x) - x_start;
-            const float wr[4] = {rA.y, rA.z, rA.w, rB.x};
             const float wc[4] = {cA.y, cA.z, cA.w, cB.x};
-            const float2* gp = grad + r0 * G::IW + c0;
+            const float2* rp = rb + s * G::IW + c0;
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-              float ax = 0.f, ay = 0.f;
-#pragma unroll
-              for (int t = 0; t < 4; ++t) {
-                const float2 g = gp[t * G::IW + u];
-                ax = fmaf(g.x, wr[t], ax);
-                ay = fmaf(g.y, wr[t], ay);
-              }
-              vgx = fmaf(ax, wc[u], vgx);
-              vgy = fmaf(ay, wc[u], vgy);
+              const float2 a = rp[u];
+              vgx = fmaf(a.x, wc[u], vgx);
+              vgy = fmaf(a.y, wc[u], vgy);
             }
             const float g2 = vgx * vgx + vgy * vgy;
             if (g2 != 0.f) {
