@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
       if (row_ok && nx < w && i >= lo_i && i < hi_i) {
         const float4* crow = reinterpret_cast<const float4*>(ct) + (px * 2) * 32 + lane;
         float div = 0.f;
-#pragma unroll 4
+#pragma unroll  // all 12 ring points in flight (measured 4.5 % faster than 4)
         for (int s = 0; s < kRing; ++s) {
           const float4 rB = *reinterpret_cast<const float4*>(rrow + s * 8 + 4);
           const float4 cA = crow[(s * M * 2) * 32];
