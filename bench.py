@@ -409,7 +409,12 @@ def run_gpu_arm(args):
         torch.cuda.empty_cache()
         line["sweep"] = bench_sweep(dev)
         torch.cuda.empty_cache()
-        line["served"] = bench_served(dev)
+        # arrival-rate sweep of the served stream; "served" is the highest rate
+        sweep = [bench_served(dev, rate=r) for r in (5.0, 50.0, 200.0)]
+        line["served_sweep"] = [{"rate_per_s": r, "served": x["served"], "plain": x["plain"],
+                                 "throughput_ratio": x["throughput_ratio"]}
+                                for r, x in zip((5.0, 50.0, 200.0), sweep)]
+        line["served"] = sweep[-1]
         torch.cuda.empty_cache()
         line["srrf"] = bench_srrf(dev, stack_np)
     if not args.no_cpu_baseline:
