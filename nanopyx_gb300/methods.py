@@ -100,6 +100,28 @@ def eSRRF(image, magnification: int = 5, radius: float = 1.5, sensitivity: float
     return parts[0] if isinstance(temporal_correlation, str) else tuple(parts)
 
 
+def upload_segments(T: int, fpt: int):
+    """Frame ranges uploaded per timepoint by the host-buffer eSRRF path.
+
+    A timepoint goes up whole when there are at least three (one segment
+    overlaps the previous timepoint's compute), else in quarters; the first
+    timepoint starts with a head of ~1/5 of its frames so that the device
+    starts early.  Returns, per timepoint, a list of (first, end) frame indices
+    that tile [0, T).
+    """
+    n_tp = T // fpt + (1 if T % fpt else 0)
+    nseg = 1 if n_tp >= 3 else min(4, fpt)
+    seg_len = -(-fpt // nseg)
+    head = fpt // 5 if nseg == 1 and fpt >= 10 else seg_len
+    segs = []
+    for tp in range(n_tp):
+        a0, a1 = tp * fpt, min(T, (tp + 1) * fpt)
+        cuts = [a0 + head] if tp == 0 and head < seg_len else []
+        cuts += list(range(a0 + seg_len, a1, seg_len)) + [a1]
+        segs.append(list(zip([a0] + cuts[:-1], cuts)))
+    return segs
+
+
 def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_timepoint,
                 names, doIntensityWeighting, macro_pixel_correction) -> np.ndarray:
     """eSRRF with host buffers, copies overlapped with compute.
@@ -135,18 +157,8 @@ def _esrrf_host(arr: np.ndarray, magnification, radius, sensitivity, frames_per_
     comp = torch.cuda.current_stream(dev)
     cp = torch.cuda.Stream(dev)   # host -> device
     cpo = torch.cuda.Stream(dev)  # device -> host (never queues behind an upload)
-    nseg = 1 if n_tp >= 3 else min(4, fpt)
-    seg_len = -(-fpt // nseg)
-    max_seg = min(seg_len, T)
-    # the first timepoint goes up as a short head segment and the rest, so the
-    # device starts after ~1/5 of a timepoint has been staged
-    head = fpt // 5 if nseg == 1 and fpt >= 10 else seg_len
-    segs = []  # per timepoint: segment bounds [(sa, sb), ...]
-    for tp in range(n_tp):
-        a0, a1 = tp * fpt, min(T, (tp + 1) * fpt)
-        cuts = [a0 + head] if tp == 0 and head < seg_len else []
-        cuts += list(range(a0 + seg_len, a1, seg_len)) + [a1]
-        segs.append(list(zip([a0] + cuts[:-1], cuts)))
+    segs = upload_segments(T, fpt)
+    max_seg = max(sb - sa for tsegs in segs for sa, sb in tsegs)
     ws_push = workspace(max(L.nx_esrrf_push_workspace_bytes(plan.handle, n)
                             for n in {sb - sa for tsegs in segs for sa, sb in tsegs}), dev)
     ws_fin = workspace(256 + L.nx_macro_pixel_workspace_bytes(3, m), dev)

@@ -76,3 +76,33 @@ def test_synthetic_generator_deterministic_and_plausible():
     # background 100 photons/px: median close to 100
     assert 95 < float(np.median(a)) < 106
     assert synthetic.emitters_for_density(100, 100, 0.006) == 60
+
+
+@pytest.mark.parametrize("T,fpt", [(500, 100), (450, 100), (23, 23), (30, 12), (7, 3), (1, 1),
+                                   (10, 10), (100, 100), (99, 33)])
+def test_upload_segments_tile_the_stack(T, fpt):
+    segs = methods.upload_segments(T, fpt)
+    n_tp = -(-T // fpt)
+    assert len(segs) == n_tp
+    flat = [s for tsegs in segs for s in tsegs]
+    assert flat[0][0] == 0 and flat[-1][1] == T
+    assert all(a < b for a, b in flat)
+    assert all(flat[i][1] == flat[i + 1][0] for i in range(len(flat) - 1))
+    for tp, tsegs in enumerate(segs):  # segments never straddle a timepoint
+        assert tsegs[0][0] == tp * fpt and tsegs[-1][1] == min(T, (tp + 1) * fpt)
+
+
+def test_parallel_host_copy_handles_strided_views():
+    from nanopyx_gb300 import _hostio
+
+    rng = np.random.default_rng(3)
+    src = rng.random((7, 300, 200), dtype=np.float32)
+    dst = np.empty_like(src)
+    _hostio.par_copy(dst, src)
+    assert np.array_equal(dst, src)
+    res = np.zeros((2, 5, 400, 300), np.float32)
+    out = rng.random((2, 400, 300), dtype=np.float32)
+    _hostio.par_copy(res[:, 3], out)
+    assert np.array_equal(res[:, 3], out) and not res[:, :3].any() and not res[:, 4:].any()
+    with pytest.raises(ValueError):
+        _hostio.par_copy(dst[:3], src)
