@@ -823,7 +823,12 @@ __global__ void __launch_bounds__(32 * TY * M + kProducerThreads, EsrrfTile<M>::
           }
         }
         if (MODE == kModeSum) {
-          for (int k = 0; k < p.n_sens; ++k) {
+          // unrolled over the sensitivity slots (a runtime-bounded loop here
+          // made the compiler re-materialise addresses in the RGC core: +14 %
+          // instructions)
+#pragma unroll
+          for (int k = 0; k < kMaxSens; ++k) {
+            if (k >= p.n_sens) break;
             float2* ks = reinterpret_cast<float2*>(tk) + (k * M + px) * G::NTC + tid;
             float kv = 0.f, sv = 0.f;
             if (!first) {
