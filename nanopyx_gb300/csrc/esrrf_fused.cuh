@@ -101,10 +101,15 @@ struct EsrrfTile {
   // spilling (m = 5: 20 consumer + 4 producer warps at 80 registers measured
   // 12 % faster than 15 + 4 at 96, 40 % faster than 10 + 4)
   static constexpr int TY = (M <= 2) ? 8 : (M <= 3 ? 4 : (M == 4 ? 3 : (M == 5 ? 4 : (M == 6 ? 2 : 1))));
-  static constexpr int NT = 32 * TY * M + 128;
-  static constexpr int MIN_BLOCKS = (M <= 2 && NT <= 384) ? 2 : 1;
+  // producer threads: the preparation per input pixel is the same for every m
+  // while the RGC work grows with m^2, so small m needs more producers.
+  // Measured (200 x 512 x 512, VAR): m = 5 best with one warpgroup (96 or 64
+  // threads slower); m = 2: 6.31 / 4.74 / 4.15 / 4.23 ms with 128 / 256 / 384 /
+  // 512; m = 3: 9.23 / 7.60 / 7.75 ms with 128 / 256 / 384.
+  static constexpr int NP = (M <= 2) ? 384 : (M == 3 ? 256 : 128);
+  static constexpr int NT = 32 * TY * M + NP;
+  static constexpr int MIN_BLOCKS = (NT <= 384) ? 2 : 1;
 };
-constexpr int kProducerThreads = 128;  // one warpgroup (96 or 64 measured slower)
 
 // Frames per pass (FP).  With FP = 2 a consumer carries two consecutive frames
 // through each pass: the RGC core runs on packed f32x2 arithmetic (frame pair
@@ -136,7 +141,7 @@ struct Geo {
   static constexpr int OX = TX * M;
   static constexpr int RIW = TX + 4;
   static constexpr int NTC = 32 * TY * M;        // consumer threads
-  static constexpr int NP = kProducerThreads;    // producer threads
+  static constexpr int NP = EsrrfTile<M>::NP;    // producer threads
   static constexpr int NT = NTC + NP;
   // phase-table block per (py, jj), in float4:
   //   FP = 1: a[NS4] b[NS4] w[NS4]   (4 samples per float4)
@@ -480,7 +485,7 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
 }
 
 template <int M, int J, int TY, int FP, int MODE>
-__global__ void __launch_bounds__(32 * TY * M + kProducerThreads, EsrrfTile<M>::MIN_BLOCKS)
+__global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::MIN_BLOCKS)
     esrrf_fused_kernel(const __grid_constant__ TmapPack maps, const UnitTable ut) {
   using G = Geo<M, J, TY, FP>;
   extern __shared__ __align__(128) float sm[];
