@@ -100,13 +100,15 @@ struct EsrrfTile {
   // rows per tile: as many consumer warps as the registers allow without
   // spilling (m = 5: 20 consumer + 4 producer warps at 80 registers measured
   // 12 % faster than 15 + 4 at 96, 40 % faster than 10 + 4)
-  static constexpr int TY = (M <= 2) ? 8 : (M <= 3 ? 4 : (M == 4 ? 3 : (M == 5 ? 4 : (M == 6 ? 2 : 1))));
+  static constexpr int TY = (M <= 2) ? 8 : (M <= 5 ? 4 : (M == 6 ? 2 : 1));
   // producer threads: the preparation per input pixel is the same for every m
   // while the RGC work grows with m^2, so small m needs more producers.
   // Measured (200 x 512 x 512, VAR): m = 5 best with one warpgroup (96 or 64
   // threads slower); m = 2: 6.31 / 4.74 / 4.15 / 4.23 ms with 128 / 256 / 384 /
-  // 512; m = 3: 9.23 / 7.60 / 7.75 ms with 128 / 256 / 384.
-  static constexpr int NP = (M <= 2) ? 384 : (M == 3 ? 256 : 128);
+  // 512; m = 3: 9.23 / 7.60 / 7.75 ms with 128 / 256 / 384; m = 4 (4 rows):
+  // 12.12 / 11.82 ms with 128 / 256 (3 rows: 12.41 / 12.48); m = 5: 16.92 /
+  // 18.11 ms with 128 / 256.
+  static constexpr int NP = (M <= 2) ? 384 : (M <= 4 ? 256 : 128);
   static constexpr int NT = 32 * TY * M + NP;
   static constexpr int MIN_BLOCKS = (NT <= 384) ? 2 : 1;
 };
