@@ -214,22 +214,17 @@ static int check_plan(const nx_esrrf_plan* p) {
 }
 
 // chunking of each timepoint's frames across CTAs (deterministic in its inputs)
-// Frame chunks per timepoint of a single-stack launch.  The resident CTAs
-// stride over (tile, timepoint, chunk) units, so a CTA runs about
-// ceil(units / resident) units, each costing its frame passes plus a start-up
-// of ~0.65 pass (the unit's first pass is not overlapped with the producer
-// warps' preparation).  The chunk count with the smallest estimate wins: few
-// chunks for large stacks, enough to fill every SM for small ones.
-static int plan_chunks(const nx_esrrf_plan* p, int T, int fpt, int n_tp) {
-  if (!p->fused) return 1;
-  const int TY = p->fused->geo.TY;
-  const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + TY - 1) / TY);
-  const int min_nf = std::min(fpt, T - (n_tp - 1) * fpt);
-  const long long resident =
-      (long long)std::max(1, p->fused->occupancy[kModeFull](1)) * device_sms();
+// Frame chunks per timepoint of a launch over `tiles` x `n_tp` units.  The
+// resident CTAs stride over (tile, timepoint, chunk) units, so a CTA runs
+// about ceil(units / resident) units, each costing its frame passes plus a
+// start-up of ~0.65 pass (the unit's first pass is not overlapped with the
+// producer warps' preparation).  The chunk count with the smallest estimate
+// wins: few chunks for large stacks, enough to fill every SM for small ones,
+// and >= 4 frames per chunk.
+static int best_chunks(long long tiles, int n_tp, int fpt, int min_nf, long long resident) {
   int best = 1;
   double best_cost = 1e300;
-  const int cmax = std::max(1, std::min(min_nf / 4, 64));  // >= 4 frames per chunk
+  const int cmax = std::max(1, std::min(min_nf / 4, 64));
   for (int c = 1; c <= cmax; ++c) {
     const long long units = tiles * n_tp * c;
     const double per_cta = (double)((units + resident - 1) / resident);
@@ -241,6 +236,16 @@ static int plan_chunks(const nx_esrrf_plan* p, int T, int fpt, int n_tp) {
     }
   }
   return best;
+}
+
+static int plan_chunks(const nx_esrrf_plan* p, int T, int fpt, int n_tp) {
+  if (!p->fused) return 1;
+  const int TY = p->fused->geo.TY;
+  const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + TY - 1) / TY);
+  const int min_nf = std::min(fpt, T - (n_tp - 1) * fpt);
+  const long long resident =
+      (long long)std::max(1, p->fused->occupancy[kModeFull](1)) * device_sms();
+  return best_chunks(tiles, n_tp, fpt, min_nf, resident);
 }
 
 static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
@@ -759,11 +764,12 @@ int nx_esrrf_batch_create(nx_esrrf_batch** out, const nx_esrrf_item* items, int 
     const int min_nf = std::min(bi.fpt, it.T - (bi.n_tp - 1) * bi.fpt);
     int fpu = it.frames_per_unit;
     if (fpu <= 0) {
-      // heuristic: enough units for ~3 waves of this item alone, >= 8 frames each
+      // heuristic: the chunking that balances this item alone over the resident CTAs
       const long long tiles = (long long)((p->W + 31) / 32) * ((p->H + p->fused->geo.TY - 1) / p->fused->geo.TY);
-      long long c = (3LL * sms + tiles * bi.n_tp - 1) / (tiles * bi.n_tp);
-      c = std::min<long long>(c, std::max(1, min_nf / 8));
-      fpu = (int)std::max<long long>(1, (min_nf + c - 1) / c);
+      const long long resident =
+          (long long)std::max(1, p->fused->occupancy[bi.mode](std::max(1, it.n_sens))) * sms;
+      const int c = best_chunks(tiles, bi.n_tp, bi.fpt, min_nf, resident);
+      fpu = std::max(1, (min_nf + c - 1) / c);
     }
     bi.chunks = std::max(1, std::min(min_nf, (min_nf + fpu - 1) / fpu));
     bi.cls = -1;
