@@ -110,7 +110,9 @@ struct EsrrfTile {
   // 18.11 ms with 128 / 256.
   static constexpr int NP = (M <= 2) ? 384 : (M <= 4 ? 256 : 128);
   static constexpr int NT = 32 * TY * M + NP;
-  static constexpr int MIN_BLOCKS = (NT <= 384) ? 2 : 1;
+  // one CTA per SM: registers for the consumers (m = 8 with 2 CTAs per SM at
+  // 80 registers measured 11 % slower than 1 CTA)
+  static constexpr int MIN_BLOCKS = 1;
 };
 
 // Frames per pass (FP).  With FP = 2 a consumer carries two consecutive frames
