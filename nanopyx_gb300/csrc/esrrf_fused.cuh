@@ -1,21 +1,25 @@
 // Fused eSRRF frame-loop kernel (sm_103a), warp-specialised.
 //
-// One CTA owns a 32 x TY tile of input pixels (= a 32M x TY*M tile of output
-// pixels), one timepoint and one contiguous chunk of that timepoint's frames.
-// Per frame it
-//   1. receives the input tile + halo by TMA (double-buffered, mbarrier), or
-//      by plain loads when the row pitch is not 16-byte aligned;
-//   2. computes Roberts-Cross gradients          (_c_gradients.c:53-73);
-//   3. Catmull-Rom-interpolates them on the half-pixel grid -- the only
+// One CTA works through units -- (stack, 32 x TY tile of input pixels = a
+// 32M x TY*M tile of output pixels, timepoint, frame chunk) -- two frames per
+// pass.  Its producer warps, per pass,
+//   1. receive the input tiles + halo by TMA (two sets of buffers, mbarrier),
+//      or by plain loads when the row pitch is not 16-byte aligned;
+//   2. compute Roberts-Cross gradients          (_c_gradients.c:53-73) and the
+//      row pass of the intensity magnification  (_c_interpolation_catmull_rom.c:21-52);
+//   3. Catmull-Rom-interpolate the gradients on the half-pixel grid -- the only
 //      positions the reference RGC ever reads from its 2m-magnified gradient
 //      images (rows/cols k*m, clamped to 2*m*H-1;
-//      _c_sr_radial_gradient_convergence.c:45-61) -- and normalises them;
-//   4. Catmull-Rom-magnifies the intensity       (_c_interpolation_catmull_rom.c:21-52);
-//   5. evaluates RGC for its M output pixels per thread with FP64-derived
-//      phase tables of the distance weights      (_c_sr_radial_gradient_convergence.c:17-90);
-//   6. applies ^sensitivity, intensity weighting and the margin, and either
-//      writes the per-frame value (eSRRF_ST stack) or folds it into per-pixel
-//      temporal sums kept in shared memory (shift K = first value; S, Q, P, L).
+//      _c_sr_radial_gradient_convergence.c:45-61) -- and normalise them into a
+//      double-buffered slot;
+// while its consumer warps, one thread per input pixel and output row phase,
+//   4. evaluate RGC for the thread's M output pixels with FP64-derived phase
+//      tables of the distance weights      (_c_sr_radial_gradient_convergence.c:17-90),
+//      on packed f32x2 arithmetic (both frames in one register pair);
+//   5. apply ^sensitivity, the intensity (column pass) and the margin, and
+//      either write the per-frame value (eSRRF_ST stack) or fold it into
+//      per-pixel temporal sums kept in shared memory (shift K = first value;
+//      S, Q, P, L).
 // Nothing of size (T, 2Hm, 2Wm) or (T, Hm, Wm) is ever materialised for the
 // temporal modes.
 #pragma once
