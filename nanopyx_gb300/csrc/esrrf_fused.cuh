@@ -281,10 +281,15 @@ struct Producer {
   }
 
   // gradient column pass onto the half-grid columns
+  // (each row's even half-grid columns first, then its odd ones, so that the
+  // lanes of a warp mostly take the same odd / even branch)
   __device__ void column_pass(const FusedParams& p, const UnitGeo& u) const {
     const int twoW = 2 * u.W;
+    constexpr int HALF = (G::HG_C + 1) / 2;
     for (int i = ptid; i < G::NRY * G::HG_C; i += G::NP) {
-      const int rl = i / G::HG_C, kxl = i % G::HG_C;
+      const int rl = i / G::HG_C, j = i - rl * G::HG_C;
+      const int kxl = j < HALF ? 2 * j : 2 * (j - HALF) + 1;
+      const int o = rl * G::HG_C + kxl;
       const int kx = u.kb_x + kxl;
       float vc[FP], vr[FP];
 #pragma unroll
@@ -327,8 +332,8 @@ struct Producer {
       }
 #pragma unroll
       for (int fr = 0; fr < FP; ++fr) {
-        t1[(2 * fr) * G::S_T1 + i] = vc[fr];
-        t1[(2 * fr + 1) * G::S_T1 + i] = vr[fr];
+        t1[(2 * fr) * G::S_T1 + o] = vc[fr];
+        t1[(2 * fr + 1) * G::S_T1 + o] = vr[fr];
       }
     }
   }
