@@ -151,6 +151,9 @@ struct Geo {
   static constexpr int NTC = 32 * TY * M;        // consumer threads
   static constexpr int NP = EsrrfTile<M>::NP;    // producer threads
   static constexpr int NT = NTC + NP;
+  // prepared passes in flight between producers and consumers (3 or 4
+  // measured no faster: the producers keep up)
+  static constexpr int NSLOT = 2;
   // phase-table block per (py, jj), in float4:
   //   FP = 1: a[NS4] b[NS4] w[NS4]   (4 samples per float4)
   //   FP = 2: (a, b, -b, w) per sample, each value broadcast into a frame pair
@@ -167,9 +170,9 @@ struct Geo {
   static constexpr int S_T1 = al(NRY * HG_C);  // column-pass gx, gy per frame
   static constexpr int O_HG = O_T1 + 2 * FP * S_T1;
   static constexpr int S_HG = al(HG_R * 2 * HGP * 2 * FP);  // one slot: float2 / float4 gradients
-  static constexpr int O_RI = O_HG + 2 * S_HG;              // two slots
+  static constexpr int O_RI = O_HG + NSLOT * S_HG;          // NSLOT slots
   static constexpr int S_RI = al(OY * RIW);  // intensity row pass per frame
-  static constexpr int O_TB = O_RI + 2 * FP * S_RI;         // two slots of FP planes
+  static constexpr int O_TB = O_RI + NSLOT * FP * S_RI;     // NSLOT slots of FP planes
   static constexpr int S_TB = al(M * W2 * TBLK * 4);
   static constexpr int O_RW = O_TB + S_TB;
   static constexpr int S_RW = al(OY * 5);
@@ -185,7 +188,7 @@ struct Geo {
   __host__ __device__ static constexpr int o_bar(int mode, int ns_cap) {
     return mode == 1 ? O_TK + 2 * ns_cap * M * NTC : (mode == 2 ? O_BAR_FULL : O_TK);
   }
-  // 5 + 2 FP mbarriers after o_bar
+  // 2 NSLOT + 1 + 2 FP (<= 11) mbarriers after o_bar
   __host__ __device__ static constexpr size_t smem_bytes(int mode, int ns_cap) {
     return size_t(o_bar(mode, ns_cap) + 32) * 4;
   }
@@ -511,10 +514,10 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
   float* tw = sm + G::O_TW;  // tw[px * NTC + tid]
   float* tk = sm + G::O_TK;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + G::o_bar(MODE, ut.ns_cap));
-  uint64_t* full = bars;       // [2] slot prepared (NP arrivals)
-  uint64_t* empty = bars + 2;  // [2] slot released (NTC arrivals)
-  uint64_t* pbar = bars + 4;   // producer-group barrier (NP arrivals)
-  uint64_t* tbar = bars + 5;   // [2 FP] TMA input tiles
+  uint64_t* full = bars;                    // [NSLOT] slot prepared (NP arrivals)
+  uint64_t* empty = bars + G::NSLOT;        // [NSLOT] slot released (NTC arrivals)
+  uint64_t* pbar = bars + 2 * G::NSLOT;     // producer-group barrier (NP arrivals)
+  uint64_t* tbar = bars + 2 * G::NSLOT + 1; // [2 FP] TMA input tiles
 
   const int tid = threadIdx.x;
   const bool producer = tid >= G::NTC;
@@ -526,17 +529,17 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
                               sm + G::O_RI, rw, tid - G::NTC};
 
   if (tid == 0) {
-    mbar_init(&full[0], G::NP);
-    mbar_init(&full[1], G::NP);
-    mbar_init(&empty[0], G::NTC);
-    mbar_init(&empty[1], G::NTC);
+    for (int k = 0; k < G::NSLOT; ++k) {
+      mbar_init(&full[k], G::NP);
+      mbar_init(&empty[k], G::NTC);
+    }
     mbar_init(pbar, G::NP);
     for (int k = 0; k < 2 * FP; ++k) mbar_init(&tbar[k], 1);
     fence_mbar_init();
     s_abort = 0;
   }
   __syncthreads();
-  unsigned gp = 0;      // frame passes since launch: slot gp & 1, use gp >> 1 (all threads)
+  unsigned gp = 0;      // frame passes since launch: slot gp % NSLOT, use gp / NSLOT (all threads)
   unsigned tphase = 0;  // producers: bit k = parity of the next completion of tbar[k]
   unsigned tpend = 0;   // producers: bit k = a TMA load into input buffer k is in flight
   unsigned pphase = 0;  // producers: parity of the next completion of pbar
@@ -707,8 +710,8 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
     }
     for (int j = 0; j < npass; ++j) {
       const unsigned g = gp + j;
-      const int s = g & 1;
-      const unsigned use = g >> 1;
+      const int s = (int)(g % G::NSLOT);
+      const unsigned use = g / G::NSLOT;
       const int fa = f0 + j * FP;
       const int set = j & 1;
       const int nf = min(FP, f1 - fa);
@@ -787,8 +790,8 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
     const size_t plane = (size_t)p.rowsM * p.colsM;
     for (int j = 0; j < npass; ++j) {
       const unsigned g = gp + j;
-      const int s = g & 1;
-      const unsigned use = g >> 1;
+      const int s = (int)(g % G::NSLOT);
+      const unsigned use = g / G::NSLOT;
       const int fa = f0 + j * FP;
       const int nf = min(FP, f1 - fa);
       if (!mbar_wait_or_abort(&full[s], use & 1u, &s_abort)) {
