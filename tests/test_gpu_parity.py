@@ -206,3 +206,14 @@ def test_srrf_fused_and_general_paths_against_oracle(m, ring, border):
     mag = O.cr_shift_magnify(x, 0, 0, m, m)
     ref = O.macro_pixel_correct(O.radiality(x, mag, m, ring, border), m)
     assert rel_err(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("m,r,corr", [(8, 2.0, "VAR"), (5, 3.0, "TAC2"), (6, 2.5, "AVG"), (8, 1.5, "AVG")])
+def test_one_frame_per_pass_instantiations_against_oracle(m, r, corr):
+    """Large windows / magnifications whose frame-pair layout does not fit shared memory run
+    one frame per pass; odd frame counts exercise the single-frame tail of a pass too."""
+    x = blinking_stack(5, 22, 34, 6, seed=m * 7 + int(r * 2))
+    got = nx.eSRRF(x, magnification=m, radius=r, sensitivity=2, temporal_correlation=corr,
+                   macro_pixel_correction=False)
+    ref = O.esrrf(x, m, r, 2, 0, corr, True, False)
+    assert rel_err(got, np.squeeze(ref)) <= TOL
