@@ -24,8 +24,9 @@ def _pool() -> cf.ThreadPoolExecutor:
     global _POOL
     with _LOCK:
         if _POOL is None:
-            _POOL = cf.ThreadPoolExecutor(max_workers=max(1, min(8, (os.cpu_count() or 2) // 2)),
-                                          thread_name_prefix="nx-hostio")
+            n = int(os.environ.get("NANOPYX_GB300_HOST_THREADS", "0")) or \
+                max(1, min(8, (os.cpu_count() or 2) // 2))
+            _POOL = cf.ThreadPoolExecutor(max_workers=n, thread_name_prefix="nx-hostio")
         return _POOL
 
 
