@@ -158,7 +158,10 @@ struct Geo {
   //   FP = 1: a[NS4] b[NS4] w[NS4]   (4 samples per float4)
   //   FP = 2: (a, b, -b, w) per sample, each value broadcast into a frame pair
   //           (measured 12 % faster than storing the pairs duplicated)
-  static constexpr int TBLK = FP == 2 ? 4 * NS4 : 3 * NS4;
+  static constexpr int TBLK = FP >= 2 ? 4 * NS4 : 3 * NS4;
+  // unit gradients of one slot: FP = 1: float2 (nx, ny) per half-grid sample;
+  // FP >= 2: one plane per frame pair of float4 (nx0, nx1, ny0, ny1)
+  static constexpr int HG_PLANE = HG_R * 2 * HGP;  // samples per plane
 
   __host__ __device__ static constexpr int al(int n) { return (n + 31) / 32 * 32; }
   // shared-memory layout (in floats, 128-byte aligned blocks)
@@ -202,6 +205,9 @@ template <int M, int J, int MODE>
 struct FusedCfg {
   static constexpr int TY = EsrrfTile<M>::TY;
   static constexpr int NSC = MODE == kModeSum ? kMaxSens : 1;
+  // FP = 4 (two frame pairs per pass sharing the table loads) is supported by
+  // the code but not selected: it does not fit shared memory with the VAR/TAC2
+  // or AVG state at m = 5, and in stack mode it measured 9 % slower.
   static constexpr int FP = Geo<M, J, TY, 2>::smem_bytes(MODE, NSC) <= kSmemBudget ? 2 : 1;
   using G = Geo<M, J, TY, FP>;
 };
@@ -399,10 +405,14 @@ struct Producer {
         }
       }
       const int o = (kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1);
-      if constexpr (FP == 2)
-        reinterpret_cast<float4*>(hgf)[o] = make_float4(nxv[0], nxv[1], nyv[0], nyv[1]);
-      else
+      if constexpr (FP >= 2) {
+#pragma unroll
+        for (int pp = 0; pp < FP / 2; ++pp)
+          reinterpret_cast<float4*>(hgf)[pp * G::HG_PLANE + o] =
+              make_float4(nxv[2 * pp], nxv[2 * pp + 1], nyv[2 * pp], nyv[2 * pp + 1]);
+      } else {
         reinterpret_cast<float2*>(hgf)[o] = make_float2(nxv[0], nyv[0]);
+      }
     }
   }
 };
@@ -457,9 +467,12 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
     // FMA-pipe operation is packed: v = w + (-|u|), acc += [dp < 0] * v
     // (measured 6 % faster than scalar v and predicated scalar adds)
     const float4* hg = reinterpret_cast<const float4*>(hgf);
-    float2 acc2[M];
+    constexpr int NPR = FP / 2;  // frame pairs per pass (share every table load)
+    float2 acc2[NPR][M];
 #pragma unroll
-    for (int px = 0; px < M; ++px) acc2[px] = make_float2(0.f, 0.f);
+    for (int pp = 0; pp < NPR; ++pp)
+#pragma unroll
+      for (int px = 0; px < M; ++px) acc2[pp][px] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int jj = 0; jj < G::W2; ++jj) {
       const int kyl = 2 * ty + cpy + jj;
@@ -471,8 +484,10 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
       // loading the row first; measured 1.3 % faster)
 #pragma unroll
       for (int q = 0; q < G::NQ; ++q) {
-        const float4 g = (q & 1) ? r1[q >> 1] : r0[q >> 1];
-        const float2 gx = make_float2(g.x, g.y), gy = make_float2(g.z, g.w);
+        float4 g[NPR];
+#pragma unroll
+        for (int pp = 0; pp < NPR; ++pp)
+          g[pp] = (q & 1) ? r1[pp * G::HG_PLANE + (q >> 1)] : r0[pp * G::HG_PLANE + (q >> 1)];
 #pragma unroll
         for (int px = 0; px < M; ++px) {
           const int ii = q - (2 * px + 1) / M;
@@ -482,21 +497,27 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
           const float2 a = make_float2(T.x, T.x), b = make_float2(T.y, T.y);
           const float2 nb = make_float2(T.z, T.z);
           const float w = T.w;
-          const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
-          const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
-          const float2 nu = make_float2(__int_as_float(__float_as_int(u.x) | 0x80000000),
-                                        __int_as_float(__float_as_int(u.y) | 0x80000000));
-          const float2 v = __fadd2_rn(make_float2(w, w), nu);
-          const float2 msk = make_float2(dp.x < 0.f ? 1.f : 0.f, dp.y < 0.f ? 1.f : 0.f);
-          acc2[px] = __ffma2_rn(msk, v, acc2[px]);
+#pragma unroll
+          for (int pp = 0; pp < NPR; ++pp) {
+            const float2 gx = make_float2(g[pp].x, g[pp].y), gy = make_float2(g[pp].z, g[pp].w);
+            const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
+            const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
+            const float2 nu = make_float2(__int_as_float(__float_as_int(u.x) | 0x80000000),
+                                          __int_as_float(__float_as_int(u.y) | 0x80000000));
+            const float2 v = __fadd2_rn(make_float2(w, w), nu);
+            const float2 msk = make_float2(dp.x < 0.f ? 1.f : 0.f, dp.y < 0.f ? 1.f : 0.f);
+            acc2[pp][px] = __ffma2_rn(msk, v, acc2[pp][px]);
+          }
         }
       }
     }
 #pragma unroll
-    for (int px = 0; px < M; ++px) {
-      acc[0][px] = acc2[px].x;
-      acc[FP - 1][px] = acc2[px].y;
-    }
+    for (int pp = 0; pp < NPR; ++pp)
+#pragma unroll
+      for (int px = 0; px < M; ++px) {
+        acc[2 * pp][px] = acc2[pp][px].x;
+        acc[2 * pp + 1][px] = acc2[pp][px].y;
+      }
   }
 }
 
@@ -829,13 +850,17 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
           float w5[5];
 #pragma unroll
           for (int k = 0; k < 5; ++k) w5[k] = cw[(lane * M + px) * 5 + k];
-          if constexpr (FP == 2) {
-            float2 s2 = make_float2(0.f, 0.f);
+          if constexpr (FP >= 2) {
 #pragma unroll
-            for (int k = 0; k < 5; ++k)
-              s2 = __ffma2_rn(make_float2(w5[k], w5[k]), make_float2(rv[0][k], rv[FP - 1][k]), s2);
-            ival[0] = s2.x;
-            ival[FP - 1] = s2.y;
+            for (int pp = 0; pp < FP / 2; ++pp) {
+              float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+              for (int k = 0; k < 5; ++k)
+                s2 = __ffma2_rn(make_float2(w5[k], w5[k]),
+                                make_float2(rv[2 * pp][k], rv[2 * pp + 1][k]), s2);
+              ival[2 * pp] = s2.x;
+              ival[2 * pp + 1] = s2.y;
+            }
           } else {
             float s1 = 0.f;
 #pragma unroll
