@@ -40,7 +40,7 @@ CFG = dict(T=500, H=512, W=512, emitters=400, m=5, radius=1.5, sensitivity=2.0,
 SMALL = dict(T=160, fpt=80)
 # DRAM bytes of one fused launch, dram__bytes_read.sum + dram__bytes_write.sum from a
 # 1-pass ncu capture of that launch (large: the full 500-frame launch; small: 160 frames)
-TRAFFIC_BYTES = {"large": 532740352 + 608213504, "small": 169642496 + 209450752}
+TRAFFIC_BYTES = {"large": 533877248 + 607634688, "small": 169263360 + 207995904}
 METRIC = "eSRRF input Mpx*frames/s"
 REF_SAMPLE_FRAMES = 4
 
