@@ -37,8 +37,7 @@ struct SrrfTile {
   static constexpr int O_IN = 0;                        // input tile
   static constexpr int O_G = O_IN + al(IH * IW);        // gradient float2 (gx, gy)
   static constexpr int O_RI = O_G + al(IH * IW * 2);    // intensity row pass
-  static constexpr int O_INT = O_RI + al(OY * RIW);     // magnified intensity
-  static constexpr int O_RW = O_INT + al(OY * OX);      // intensity row weights [OY][5]
+  static constexpr int O_RW = O_RI + al(OY * RIW);      // intensity row weights [OY][5]
   static constexpr int O_CW = O_RW + al(OY * 5);        // intensity col weights [OX][5]
   static constexpr int O_RT = O_CW + al(OX * 5);        // ring row taps [OY][12][8]
   // ring col taps: float4 halves [ring][px][2][lane] (lane-contiguous, conflict-free)
@@ -84,7 +83,6 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
   float* tin = sm + G::O_IN;
   float2* grad = reinterpret_cast<float2*>(sm + G::O_G);
   float* ri = sm + G::O_RI;
-  float* inten = sm + G::O_INT;
   float* rw = sm + G::O_RW;
   float* cw = sm + G::O_CW;
   float* rt = sm + G::O_RT;
@@ -190,18 +188,6 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
       ri[i] = sum;
     }
     __syncthreads();
-    if (p.iw && own_intensity) {
-      for (int i = tid; i < G::OY * G::OX; i += G::NT) {
-        const int oy = i / G::OX, ox = i % G::OX;
-        const float* w5 = cw + ox * 5;
-        const float* rr = ri + oy * G::RIW + ox / M;
-        float sum = 0.f;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) sum = fmaf(w5[k], rr[k], sum);
-        inten[i] = sum;
-      }
-      __syncthreads();
-    }
     // row pass of the ring interpolation: the ring points of this warp's output
     // row share their tap rows and weights, so each (ring point, tile column)
     // sum over the 4 tap rows is formed once per warp (same fma order as the
@@ -262,9 +248,19 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
         }
         div /= 12.f;
         val = p.positivity ? fmaxf(div, 0.f) : div;
-        if (p.iw)
-          val *= own_intensity ? inten[(ty * M + py) * G::OX + lane * M + px]
-                               : __ldg(p.interp + (size_t)f * plane + (size_t)j * colsM + i);
+        if (p.iw) {
+          if (own_intensity) {
+            // column pass of the intensity magnification (5 taps of the row pass)
+            const float* w5 = cw + (lane * M + px) * 5;
+            const float* rr = ri + (ty * M + py) * G::RIW + lane;
+            float sum = 0.f;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sum = fmaf(w5[k], rr[k], sum);
+            val *= sum;
+          } else {
+            val *= __ldg(p.interp + (size_t)f * plane + (size_t)j * colsM + i);
+          }
+        }
       }
       if (ny < h && nx < w) p.out[(size_t)f * plane + (size_t)j * colsM + i] = val;
     }
