@@ -16,17 +16,18 @@ import numpy as np
 import torch
 
 _POOL = None
+_WORKERS = 1
 _LOCK = threading.Lock()
 _MIN_PART = 1 << 21  # bytes per copy task
 
 
 def _pool() -> cf.ThreadPoolExecutor:
-    global _POOL
+    global _POOL, _WORKERS
     with _LOCK:
         if _POOL is None:
-            n = int(os.environ.get("NANOPYX_GB300_HOST_THREADS", "0")) or \
+            _WORKERS = int(os.environ.get("NANOPYX_GB300_HOST_THREADS", "0")) or \
                 max(1, min(8, (os.cpu_count() or 2) // 2))
-            _POOL = cf.ThreadPoolExecutor(max_workers=n, thread_name_prefix="nx-hostio")
+            _POOL = cf.ThreadPoolExecutor(max_workers=_WORKERS, thread_name_prefix="nx-hostio")
         return _POOL
 
 
@@ -46,7 +47,7 @@ def par_copy(dst: np.ndarray, src: np.ndarray) -> None:
     if dst.shape != src.shape:
         raise ValueError(f"shape mismatch {dst.shape} vs {src.shape}")
     pool = _pool()
-    parts = int(max(1, min(pool._max_workers * 2, dst.nbytes // _MIN_PART)))
+    parts = int(max(1, min(_WORKERS * 2, dst.nbytes // _MIN_PART)))
     if parts == 1 or dst.ndim == 0:
         np.copyto(dst, src)
         return
