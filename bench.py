@@ -633,6 +633,55 @@ def bench_srrf(dev, stack_np, frames=20, repeats=2):
     return res
 
 
+def bench_standalone_ops(dev):
+    """HBM throughput of the standalone ops off the fused path: Catmull-Rom
+    ShiftAndMagnify (100 x 512 x 512, m=5) and the eSRRF temporal correlations
+    of a 100 x 2560 x 2560 stack, against the measured HBM copy bandwidth."""
+    import torch
+
+    from nanopyx_gb300 import _native as N
+
+    L = N.lib()
+    s = torch.cuda.current_stream(dev)
+    T, H, W, m = 100, 512, 512, 5
+    x = torch.rand((T, H, W), device=dev)
+    zr = torch.zeros(T, device=dev)
+    out = torch.empty((T, H * m, W * m), device=dev)
+    stack = torch.rand((T, H * m * W * m), device=dev)
+    res = torch.empty(H * m * W * m, device=dev)
+
+    def timeit(f, n=5):
+        for _ in range(2):
+            f()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(n):
+            f()
+        e1.record(s)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / n
+
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        peak = 6800.0  # fallback figure for a GB300
+    rows = []
+    ms = timeit(lambda: N.check(L.nx_cr_shift_magnify(
+        x.data_ptr(), T, H, W, zr.data_ptr(), zr.data_ptr(), 5.0, 5.0, out.data_ptr(),
+        s.cuda_stream), "cr"))
+    b = (x.numel() + out.numel()) * 4
+    rows.append({"op": "cr_shift_magnify 100x512x512 m=5", "ms": ms, "gbs": b / ms / 1e6})
+    for name, c in (("AVG", 1), ("VAR", 2), ("TAC2", 4)):
+        ms = timeit(lambda: N.check(L.nx_temporal_correlation(
+            stack.data_ptr(), T, H * m * W * m, c, res.data_ptr(), s.cuda_stream), "tc"))
+        b = (stack.numel() + res.numel()) * 4
+        rows.append({"op": f"temporal {name} 100x2560x2560", "ms": ms, "gbs": b / ms / 1e6})
+    for r in rows:
+        r["frac_of_measured_hbm"] = r["gbs"] / peak
+    return {"hbm_peak_gbs": peak, "ops": rows}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -643,6 +692,9 @@ def main():
     ap.add_argument("--srrf-only", action="store_true",
                     help="only the SRRF measurement (profiling the radiality kernel)")
     ap.add_argument("--srrf-frames", type=int, default=20)
+    ap.add_argument("--ops-only", action="store_true",
+                    help="only the HBM throughput of the standalone ShiftAndMagnify and "
+                         "temporal-correlation kernels")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the uneven-batch, sweep and served-stream measurements")
     ap.add_argument("--workload", default="large", choices=["large", "small"],
@@ -652,6 +704,12 @@ def main():
         CFG.update(SMALL)
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.ops_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_standalone_ops(torch.device("cuda", 0))), flush=True)
+        return 0
     if args.srrf_only:
         import torch
 
