@@ -24,6 +24,7 @@ import ctypes as C
 import json
 import os
 import threading
+import warnings
 
 import numpy as np
 import torch
@@ -225,9 +226,14 @@ def sweep_batch(stack, magnification: int, sensitivities, radii, frames_per_time
 # ---------------------------------------------------------------------------
 # autotuner: frames per work unit
 # ---------------------------------------------------------------------------
+# bumped whenever the kernels' tiling or unit structure changes, so that tunings
+# made with an older build are not reused
+TUNE_LAYOUT = "ws2"
+
+
 def _gpu_key():
     p = torch.cuda.get_device_properties(torch.cuda.current_device())
-    return f"{p.name}/{p.multi_processor_count}"
+    return f"{p.name}/{p.multi_processor_count}/{TUNE_LAYOUT}"
 
 
 def _load_cache():
@@ -242,6 +248,23 @@ def _cached_fpu(key) -> int:
     m, r = key
     J = int(np.float32(2.0) * np.float32(r))
     return int(_load_cache().get(_gpu_key(), {}).get(f"m{m}_J{J}", 0))
+
+
+def _store_fpu(gpu_key: str, magnification: int, J: int, fpu: int) -> bool:
+    """Record a tuned frames-per-unit; False (and a warning) if the cache is not writable."""
+    with _cache_lock:
+        data = _load_cache()
+        data.setdefault(gpu_key, {})[f"m{int(magnification)}_J{int(J)}"] = int(fpu)
+        try:
+            os.makedirs(os.path.dirname(_CACHE_PATH), exist_ok=True)
+            tmp = f"{_CACHE_PATH}.{os.getpid()}.tmp"
+            with open(tmp, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+            os.replace(tmp, _CACHE_PATH)  # atomic: concurrent tuners never see a torn file
+        except OSError as e:
+            warnings.warn(f"autotune cache not written ({e})")
+            return False
+    return True
 
 
 def tune_frames_per_unit(stack, magnification: int = 5, radius: float = 1.5,
@@ -268,10 +291,5 @@ def tune_frames_per_unit(stack, magnification: int = 5, radius: float = 1.5,
     best = min(times, key=times.get)
     if save:
         J = int(np.float32(2.0) * np.float32(radius))
-        with _cache_lock:
-            data = _load_cache()
-            data.setdefault(_gpu_key(), {})[f"m{int(magnification)}_J{J}"] = int(best)
-            os.makedirs(os.path.dirname(_CACHE_PATH), exist_ok=True)
-            with open(_CACHE_PATH, "w") as f:
-                json.dump(data, f, indent=1, sort_keys=True)
+        _store_fpu(_gpu_key(), magnification, J, best)
     return best, times

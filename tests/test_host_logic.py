@@ -106,3 +106,19 @@ def test_parallel_host_copy_handles_strided_views():
     assert np.array_equal(res[:, 3], out) and not res[:, :3].any() and not res[:, 4:].any()
     with pytest.raises(ValueError):
         _hostio.par_copy(dst[:3], src)
+
+
+def test_autotune_cache_roundtrip_and_unwritable_location(tmp_path, monkeypatch):
+    from nanopyx_gb300 import engine
+
+    path = tmp_path / "tune" / "autotune.json"
+    monkeypatch.setattr(engine, "_CACHE_PATH", str(path))
+    assert engine._store_fpu("GPU/152/x", 5, 3, 32)
+    assert engine._store_fpu("GPU/152/x", 4, 2, 16)
+    data = engine._load_cache()
+    assert data["GPU/152/x"] == {"m5_J3": 32, "m4_J2": 16}
+    blocker = tmp_path / "file"
+    blocker.write_text("")
+    monkeypatch.setattr(engine, "_CACHE_PATH", str(blocker / "sub" / "autotune.json"))
+    with pytest.warns(UserWarning):
+        assert not engine._store_fpu("GPU/152/x", 5, 3, 8)
