@@ -80,3 +80,25 @@ def test_weight_table_rejects_bad_args(lib):
     assert lib.nx_esrrf_weight_table(0, 1.5, None, 0) == _native.NX_ERR_INVALID_ARG
     assert lib.nx_esrrf_weight_table(5, -1.0, None, 0) == _native.NX_ERR_INVALID_ARG
     assert "radius" in lib.nx_last_error().decode()
+
+
+def test_argument_checks_run_before_any_device_work(lib):
+    """Entry points reject bad arguments on the host, before touching a device."""
+    P = ctypes.c_void_p
+    # the failure-detection self-test needs a status workspace and a short limit
+    assert lib.nx_selftest_wait_timeout(None, 0, 1000, None) == _native.NX_ERR_WORKSPACE
+    assert lib.nx_selftest_wait_timeout(P(256), 64, 1000, None) == _native.NX_ERR_WORKSPACE
+    assert lib.nx_selftest_wait_timeout(P(256), 256, 2_000_000_000, None) == \
+        _native.NX_ERR_INVALID_ARG
+    # temporal correlation: shape and correlation code
+    assert lib.nx_temporal_correlation(None, 0, 10, _native.NX_CORR_AVG, None, None) == \
+        _native.NX_ERR_INVALID_ARG
+    assert lib.nx_temporal_correlation(None, 5, 10, 3, None, None) == _native.NX_ERR_INVALID_ARG
+    # allocation-free macro-pixel correction: shape, magnification, static scratch size
+    assert lib.nx_macro_pixel_correct_static(None, 1, 10, 10, 5, None) == \
+        _native.NX_ERR_INVALID_ARG
+    assert lib.nx_macro_pixel_correct_static(P(256), 1, 10, 10, 0, None) == \
+        _native.NX_ERR_INVALID_ARG
+    assert lib.nx_macro_pixel_correct_static(P(256), 100000, 10, 10, 5, None) == \
+        _native.NX_ERR_INVALID_ARG
+    assert b"static scratch" in lib.nx_last_error()
