@@ -64,27 +64,37 @@ def make_stack():
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed
+    region runs (read through a pipe; nothing is written to disk)."""
+
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
+    def __init__(self, gpu_index: int, command=None):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu_index}.csv")
+        self.thread = None
+        self.lines = []
+        self.command = command or ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}",
+                                   "--format=csv,noheader,nounits", "-lms", "100"]
+
+    def _read(self, ready):
+        for line in self.proc.stdout:
+            self.lines.append(line)
+            ready.set()
 
     def __enter__(self):
+        import threading
+
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
-                stdout=self.f, stderr=subprocess.DEVNULL)
+            self.proc = subprocess.Popen(self.command, stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            ready = threading.Event()
+            self.thread = threading.Thread(target=self._read, args=(ready,), daemon=True)
+            self.thread.start()
             # nvidia-smi takes a moment to start: hold the timed region until it samples
-            t0 = time.time()
-            while time.time() - t0 < 1.0 and os.path.getsize(self.path) == 0:
-                time.sleep(0.01)
+            ready.wait(1.0)
         except Exception:
             self.proc = None
         return self
@@ -96,19 +106,20 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-            self.f.close()
+            if self.thread is not None:
+                self.thread.join(timeout=5)
 
     def summary(self):
-        try:
-            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines()]
-        except Exception:
-            return None
+        rows = [r.strip().split(", ") for r in list(self.lines) if r.strip()]
         rows = [r for r in rows if len(r) >= 9]
         if not rows:
             return None
-        sm = [float(r[1]) for r in rows]
-        mx = max(float(r[2]) for r in rows)
-        busy = [s for s in sm if s > 0.5 * mx] or sm
+        try:
+            sm = [float(r[1]) for r in rows]
+            mx = max(float(r[2]) for r in rows)
+        except ValueError:
+            return None
+        busy = [x for x in sm if x > 0.5 * mx] or sm
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": reasons,

@@ -26,7 +26,7 @@ extern "C" {
 /* status codes */
 #define NX_OK 0
 #define NX_ERR_INVALID_ARG (-1)     /* bad shape / parameter (reference: ValueError) */
-#define NX_ERR_UNSUPPORTED (-2)     /* valid request this build does not implement */
+#define NX_ERR_UNSUPPORTED (-2)     /* valid request this library does not implement */
 #define NX_ERR_OUT_OF_MEMORY (-3)   /* device allocation failed (reference: cl.MemoryError retry) */
 #define NX_ERR_CUDA (-4)            /* CUDA runtime error */
 #define NX_ERR_DEVICE_TIMEOUT (-5)  /* a bounded device wait ran out (kernel returned early) */

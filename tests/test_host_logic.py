@@ -122,3 +122,26 @@ def test_autotune_cache_roundtrip_and_unwritable_location(tmp_path, monkeypatch)
     monkeypatch.setattr(engine, "_CACHE_PATH", str(blocker / "sub" / "autotune.json"))
     with pytest.warns(UserWarning):
         assert not engine._store_fpu("GPU/152/x", 5, 3, 8)
+
+
+def test_clock_sampler_reads_samples_through_a_pipe():
+    import sys
+    import time
+
+    import bench
+
+    fake = ("import time\n"
+            "for k in range(100):\n"
+            "    print('0, %d, 2070, 900.5, 0x0, Not Active, Not Active, Not Active, %s' % "
+            "(2070 if k % 3 else 1995, 'Active' if k == 1 else 'Not Active'), flush=True)\n"
+            "    time.sleep(0.05)\n")
+    cs = bench.ClockSampler(0, command=[sys.executable, "-c", fake])
+    with cs:
+        time.sleep(0.3)
+    s = cs.summary()
+    assert s is not None and s["samples"] >= 3
+    assert s["sm_max_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"]
+    missing = bench.ClockSampler(0, command=["no-such-sampler-binary"])
+    with missing:
+        pass
+    assert missing.summary() is None
