@@ -20,6 +20,8 @@ inside the reference project):
 * ``esrrf_st``  -- ``src/nanopyx/core/transform/_le_esrrf.pyx:172-196``.
 * ``temporal_correlation``  --
   ``src/nanopyx/core/transform/sr_temporal_correlations.py:46-75,205-221``.
+* ``acrf_lag_levels`` / ``srrf_acrf_integrated``  -- the ACRF with lag-time
+  integration, ``sr_temporal_correlations.py:111-121,159-200``.
 * ``macro_pixel_correct``  -- ``src/nanopyx/core/transform/mpcorrector.pyx:26-73``.
 * ``esrrf``  -- ``src/nanopyx/methods/esrrf/eSRRF_workflow.py:58-121``.
 * ``gradient_radiality`` / ``radiality`` / ``srrf``  --
@@ -296,6 +298,77 @@ def temporal_correlation(stack, correlation):
         c = x - x.mean(axis=0)
         return (c[:-1] * c[1:]).mean(axis=0)
     raise ValueError("Type of correlation must be AVG, VAR or TAC2")
+
+
+def acrf_lag_levels(T, order):
+    """Loop control of the reference's ACRF with lag-time integration
+    (``sr_temporal_correlations.py:159-200``), replayed without the data.
+
+    Returns one ``(n_iter, n_bin, n_binned)`` per level: the level runs
+    ``t = 0 .. n_iter - 1`` (``t < n_binned - order``), re-bins frame ``t`` for
+    ``t < n_bin`` (``t * order < n_binned``) and divides by ``n_binned`` (the
+    frame count ``T`` at the first level, then ``T / order**k`` as a Python
+    float).  Raises ``IndexError`` exactly where the reference's binning would
+    read past the last frame (``im[t * order + order - 2]`` with that index
+    ``>= T``: orders 3 and 4 at many frame counts).
+    """
+    levels = []
+    n_b = T
+    while n_b > order:
+        t, n_bin = 0, 0
+        while t < n_b - order:
+            if t * order < n_b:
+                if t * order + order - 2 >= T:
+                    raise IndexError(f"index {t * order + order - 2} is out of bounds for "
+                                     f"axis 0 with size {T}")
+                n_bin = t + 1
+            t += 1
+        levels.append((t, n_bin, n_b))
+        n_b = n_b / order
+    return levels
+
+
+def srrf_acrf_integrated(stack, order):
+    """ACRF of order 2, 3 or 4 with lag-time integration, float64 arithmetic,
+    the reference's steps (``sr_temporal_correlations.py:111-121,159-200``):
+    per level, the lag products over ``t < n_binned - order`` (``ab`` restarts
+    at each level; ``abc`` and the order-4 sums run on across levels), then
+    frame ``t`` is replaced by ``sum_{k < order-1} frame[t*order + k] / order``
+    (in place, after being zeroed, for ``t * order < n_binned``; else 0); the
+    last level's ``|ab|`` (order 2), ``|abc|`` (3) or
+    ``|abcd - ab cd - ac bd - ad bc|`` (4) over ``n_binned`` is the result
+    (zeros when no level runs)."""
+    im = np.array(stack, dtype=np.float64)
+    T = im.shape[0]
+    levels = acrf_lag_levels(T, order)
+    mean = im.mean(axis=0)
+    z = np.zeros(im.shape[1:])
+    out = z.copy()
+    abc, abcd, cd, ac, bd, ad, bc = (z.copy() for _ in range(7))
+    for n_iter, n_bin, n_b in levels:
+        ab = z.copy()
+        for t in range(n_iter):
+            a = im[t] - mean
+            b = im[t + 1] - mean
+            ab = ab + a * b
+            if order == 3:
+                abc = abc + a * b + (im[t + 2] - mean)
+            if order == 4:
+                c = im[t + 2] - mean
+                d = im[t + 3] - mean
+                abcd = abcd + a * b * c * d
+                cd, ac, bd, ad, bc = cd + c * d, ac + a * c, bd + b * d, ad + a * d, bc + b * c
+            im[t] = 0.0
+            if t < n_bin:
+                for k in range(order - 1):
+                    im[t] = im[t] + im[t * order + k] / order
+        if order == 3:
+            out = np.abs(abc) / n_b
+        elif order == 4:
+            out = np.abs(abcd - ab * cd - ac * bd - ad * bc) / n_b
+        else:
+            out = np.abs(ab) / n_b
+    return out
 
 
 def macro_pixel_correct(img, magnification):

@@ -49,7 +49,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 STAGE = os.path.join(REF_OUT, "stage")
 PKG = os.path.join(REF_OUT, "pkg")
-REFERENCE_ROOT = os.environ.get("NANOPYX_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $NANOPYX_REFERENCE_ROOT, else a directory named
+# `reference` beside this repository's root (the layout the recipe is used
+# with); without either, only an already staged tree can be compiled.
+REFERENCE_ROOT = os.environ.get("NANOPYX_REFERENCE_ROOT") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
 
 PYX_MODULES = [
     "_le_interpolation_catmull_rom",

@@ -116,6 +116,15 @@ def main():
     for order in (0, 1, -1, 2, 3, 4):
         g[f"srrf_temporal/{order}"] = np.asarray(
             R["calculate_SRRF_temporal_correlations"](xs, order), dtype=np.float32)
+    # ACRF with lag-time integration (sr_temporal_correlations.py:159-200) at frame
+    # counts the reference accepts (orders 3 and 4 raise IndexError at others)
+    rng_lag = np.random.default_rng(17)
+    for T, orders in ((12, (2, 3, 4)), (39, (3,)), (40, (2, 4))):
+        xl = (rng_lag.random((T, 8, 10)) * 2 - 0.5).astype(np.float32)
+        g[f"srrf_lag/{T}/input"] = xl
+        for order in orders:
+            g[f"srrf_lag/{T}/{order}"] = np.asarray(
+                R["calculate_SRRF_temporal_correlations"](xl, order, True), dtype=np.float32)
 
     # macro-pixel correction
     x = (rng.random((2, 20, 25)) + 0.1).astype(np.float32)

@@ -69,6 +69,30 @@ def test_oracle_temporal_and_mpc(golden):
     assert rel_err(O.macro_pixel_correct(x, 5), golden["mpc/5"]) <= 1e-5
 
 
+LAG_CASES = [(12, 2), (12, 3), (12, 4), (39, 3), (40, 2), (40, 4)]
+
+
+@pytest.mark.parametrize("T,order", LAG_CASES)
+def test_oracle_acrf_lag_integration(golden, T, order):
+    got = O.srrf_acrf_integrated(golden[f"srrf_lag/{T}/input"], order)
+    assert rel_err(got, golden[f"srrf_lag/{T}/{order}"]) <= 1e-5
+
+
+def test_oracle_lag_schedule_reproduces_the_reference_index_errors():
+    """Orders 3 and 4 raise IndexError at these frame counts in the reference
+    (its binning reads frame t*order + order - 2 past the end); order 2 never."""
+    fails = {3: [7, 10, 13, 16, 19, 22, 25, 28, 31, 34, 37, 40],
+             4: [6, 9, 10, 13, 14, 17, 18, 21, 22, 25, 26, 29, 30, 33, 34, 37, 38]}
+    for order in (2, 3, 4):
+        got = []
+        for T in range(1, 41):
+            try:
+                O.acrf_lag_levels(T, order)
+            except IndexError:
+                got.append(T)
+        assert got == fails.get(order, []), order
+
+
 def test_oracle_rejects_bad_correlation():
     with pytest.raises(ValueError):
         O.temporal_correlation(np.zeros((2, 3, 3)), "MAX")
