@@ -31,6 +31,7 @@ extern "C" {
 #define NX_ERR_CUDA (-4)            /* CUDA runtime error */
 #define NX_ERR_DEVICE_TIMEOUT (-5)  /* a bounded device wait ran out (kernel returned early) */
 #define NX_ERR_WORKSPACE (-6)       /* workspace missing or too small */
+#define NX_ERR_INDEX (-7)           /* the reference would index past its input (reference: IndexError) */
 
 /* temporal correlations (bit mask; outputs are written in this order) */
 #define NX_CORR_AVG 1
@@ -98,6 +99,19 @@ int nx_esrrf_run_stage2(const nx_esrrf_plan* plan, int T, int frames_per_timepoi
 int nx_selftest_wait_timeout(void* d_ws, size_t ws_bytes, unsigned long long limit_ns,
                              void* stream);
 
+/* Failure-detection self-test of the fused eSRRF kernel itself (not a
+ * reference routine): runs nx_esrrf_st's launch with every producer/consumer
+ * wait bounded by `limit_ns` (1 ms .. 1 s) and with the producers withholding
+ * the `full` arrival of each CTA's first frame pass.  The consumers' bounded
+ * wait runs out, the CTA raises its abort flag, every other wait of the CTA
+ * gives up, the producer leader waits (bounded) for its TMA copies in flight
+ * and the CTA returns; the time-out is recorded in the status word of `d_ws`
+ * (nx_workspace_status -> NX_ERR_DEVICE_TIMEOUT) and the context stays usable.
+ * `d_out` (T, H*m, W*m) receives whatever the aborted CTAs wrote before.     */
+int nx_selftest_fused_abort(const nx_esrrf_plan* plan, const float* d_in, int T, float* d_out,
+                            void* d_ws, size_t ws_bytes, unsigned long long limit_ns,
+                            void* stream);
+
 /* Throughput probe (not a reference routine): `blocks` CTAs of 256 threads
  * each run `iters` iterations of 8 independent FP32 FMA chains; returns via
  * d_sink (blocks*256 floats) so nothing is optimised away.  Used to measure
@@ -127,8 +141,11 @@ int nx_esrrf_accum_finalize(const nx_esrrf_plan* plan, const void* d_accum, int 
  * class (m, window), each CTA taking (stack, tile, timepoint, frame chunk)
  * units from a shared work list.  create() plans the work, bind() uploads the
  * work lists into the caller's workspace (synchronises `stream`; not
- * capturable), launch() issues kernels only -- it can be captured into a CUDA
- * graph and replayed while the buffers stay in place.
+ * capturable; creates one side stream per kernel class after the first),
+ * launch() issues kernels only -- each class's kernel, finalisation and
+ * macro-pixel correction on its own stream, forked from and joined back into
+ * `stream` by events, so class tails overlap -- and can be captured into a
+ * CUDA graph and replayed while the buffers stay in place.
  * Replaces the reference's per-stack loop (eSRRF_workflow.py:76-112) and
  * the per-(R, s) loop of the parameter sweep (core/analysis/parameter_sweep.py:33-37).
  * ------------------------------------------------------------------------ */
@@ -211,6 +228,19 @@ int nx_temporal_correlation(const float* d_stack, int T, long long n_pixels, int
 int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n_pixels, int order,
                                  float* d_out, void* stream);
 
+/* SRRF ACRF of order 2, 3 or 4 WITH lag-time integration (the reference's
+ * do_integrate_lag_times=1 branch): per level the lag products, then the
+ * frames re-binned in place by `order`, until at most `order` binned frames
+ * remain; the result is the last level's correlation (float32, the
+ * reference's operation order).  The workspace holds a working copy of the
+ * stack (the input is not modified).  Frame counts at which the reference's
+ * binning reads past its last frame (orders 3 and 4) return NX_ERR_INDEX
+ * before anything is launched, as the reference raises IndexError.
+ *   src/nanopyx/core/transform/sr_temporal_correlations.py:111-121,159-200  */
+size_t nx_srrf_acrf_workspace_bytes(int T, long long n_pixels);
+int nx_srrf_acrf_integrated(const float* d_stack, int T, long long n_pixels, int order,
+                            float* d_out, void* d_ws, size_t ws_bytes, void* stream);
+
 /* Macro-pixel correction in place on (S, rowsM, colsM).
  *   src/nanopyx/core/transform/mpcorrector.pyx:7-73                         */
 size_t nx_macro_pixel_workspace_bytes(int S, int magnification);
@@ -222,10 +252,15 @@ int nx_macro_pixel_correct(float* d_img, int S, int rowsM, int colsM, int magnif
  * (real-time acquisition loops that reserve everything at start-up, hosts whose
  * own allocator owns the GPU): same result as nx_macro_pixel_correct, with the
  * scratch in a 256 KiB device array owned by the library (held on every GPU
- * that loads it, until exit).  Calls needing more scratch than that
- * (nx_macro_pixel_workspace_bytes(S, m) > 262144) return NX_ERR_INVALID_ARG.
- * The first call on a device resolves the array's address and must come
- * before any stream capture; calls that overlap on the GPU race on the array. */
+ * that loads it, until exit).  A call needs
+ * max(S,1) * m^2 * min(64, max(1, rowsM / m)) * 4 bytes of it (S * m^2 <= 1024
+ * once rowsM >= 64 m); a larger call returns NX_ERR_INVALID_ARG and launches
+ * nothing.  The first call on a device resolves the array's address and, under
+ * lazy module loading, loads the library's kernels there and reserves the
+ * array (it may then fail with NX_ERR_OUT_OF_MEMORY): make it at start-up,
+ * before the allocation-free phase and before any stream capture.  Calls that
+ * overlap on the GPU race on the array; do not call again after a reset of
+ * the device in the same process.                                           */
 int nx_macro_pixel_correct_static(float* d_img, int S, int rowsM, int colsM, int magnification,
                                   void* stream);
 

@@ -20,6 +20,7 @@ NX_ERR_OUT_OF_MEMORY = -3
 NX_ERR_CUDA = -4
 NX_ERR_DEVICE_TIMEOUT = -5
 NX_ERR_WORKSPACE = -6
+NX_ERR_INDEX = -7
 
 NX_CORR_AVG = 1
 NX_CORR_VAR = 2
@@ -66,6 +67,7 @@ _SIGS = {
     "nx_esrrf_run_stage1": (_I, [_P, _P, _I, _I, _I, _P, _SZ, _P]),
     "nx_esrrf_run_stage2": (_I, [_P, _I, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_selftest_wait_timeout": (_I, [_P, _SZ, C.c_ulonglong, _P]),
+    "nx_selftest_fused_abort": (_I, [_P, _P, _I, _P, _P, _SZ, C.c_ulonglong, _P]),
     "nx_probe_ffma": (_I, [_P, _I, _I, _P]),
     "nx_probe_ffma2": (_I, [_P, _I, _I, _P]),
     "nx_esrrf_accum_bytes": (_SZ, [_P]),
@@ -87,6 +89,8 @@ _SIGS = {
     "nx_srrf": (_I, [_P, _I, _I, _I, _I, _FL, _I, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_temporal_correlation": (_I, [_P, _I, _LL, _I, _P, _P]),
     "nx_srrf_temporal_correlation": (_I, [_P, _I, _LL, _I, _P, _P]),
+    "nx_srrf_acrf_workspace_bytes": (_SZ, [_I, _LL]),
+    "nx_srrf_acrf_integrated": (_I, [_P, _I, _LL, _I, _P, _P, _SZ, _P]),
     "nx_macro_pixel_workspace_bytes": (_SZ, [_I, _I]),
     "nx_macro_pixel_correct": (_I, [_P, _I, _I, _I, _I, _P, _SZ, _P]),
     "nx_macro_pixel_correct_static": (_I, [_P, _I, _I, _I, _I, _P]),
@@ -145,4 +149,6 @@ def check(rc: int, what: str = "") -> None:
         raise DeviceTimeoutError(text)
     if rc == NX_ERR_UNSUPPORTED:
         raise NotImplementedError(text)
+    if rc == NX_ERR_INDEX:
+        raise IndexError(text)
     raise RuntimeError(f"{text} (status {rc})")

@@ -258,7 +258,7 @@ static int corr_count(int mask) {
 }
 
 static int fields_for(int corr_mask) {
-  return (corr_mask & (NX_CORR_VAR | NX_CORR_TAC2)) ? 5 : 2;
+  return (corr_mask & (NX_CORR_VAR | NX_CORR_TAC2)) ? 5 : 1;
 }
 
 static void fill_params(const nx_esrrf_plan* p, FusedParams& fp, const float* in, int T, int fpt,
@@ -302,11 +302,14 @@ static long long fused_units(const FusedParams& fp) {
 
 static int launch_fused_mode(const nx_esrrf_plan* p, int mode, const float* d_in, int T, int fpt,
                              int n_tp, int chunks, float* out, unsigned* status,
-                             cudaStream_t s) {
+                             cudaStream_t s, unsigned long long wait_ns = 0,
+                             int withhold_full = 0) {
   UnitTable ut;
   memset(&ut, 0, sizeof(ut));
   fill_params(p, ut.single, d_in, T, fpt, n_tp, chunks, out, status);
-  ut.single.F = mode == kModeFull ? 5 : (mode == kModeSum ? 2 : 0);
+  ut.single.F = mode_fields(mode);
+  ut.single.wait_ns = wait_ns;
+  ut.single.test_withhold_full = withhold_full;
   TmapPack pack;
   memset(&pack, 0, sizeof(pack));
   if (!tma_disabled() && make_frame_tmap(&pack.m[0], d_in, T, p->H, p->W, p->fused->geo.BW,
@@ -489,6 +492,25 @@ int nx_esrrf_st(const nx_esrrf_plan* p, const float* d_in, int T, float* d_out, 
     if (rc) return rc;
   }
   return NX_OK;
+}
+
+int nx_selftest_fused_abort(const nx_esrrf_plan* p, const float* d_in, int T, float* d_out,
+                            void* d_ws, size_t ws_bytes, unsigned long long limit_ns,
+                            void* stream) {
+  int rc = check_plan(p);
+  if (rc) return rc;
+  if (!p->fused) return invalid("the self-test needs a plan with a fused kernel");
+  if (T < 1 || !d_in || !d_out) return invalid("need frames and buffers");
+  if (limit_ns < 1000000ull || limit_ns > 1000000000ull)
+    return invalid("limit_ns must be in [1 ms, 1 s]");  // keep the self-test short
+  if (!d_ws || ws_bytes < nx_esrrf_st_workspace_bytes(p, T)) {
+    set_error("workspace too small: need %zu bytes", nx_esrrf_st_workspace_bytes(p, T));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned* status = (unsigned*)d_ws;
+  NX_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
+  return launch_fused_mode(p, kModeStack, d_in, T, T, 1, 1, d_out, status, s, limit_ns, 1);
 }
 
 size_t nx_esrrf_workspace_bytes(const nx_esrrf_plan* p, int T, int fpt, int corr_mask) {
@@ -718,6 +740,14 @@ struct nx_esrrf_batch {
   size_t counters_off = 0;
   void* d_ws = nullptr;
   int device = -1;
+  // one side stream per class after the first, and the events that fork them
+  // from / join them back into the caller's stream (created at bind)
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> events;  // [0]: fork, [1 + c]: class c done
+  ~nx_esrrf_batch() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    for (cudaStream_t st : side) cudaStreamDestroy(st);
+  }
 };
 
 namespace nx {
@@ -820,7 +850,7 @@ int nx_esrrf_batch_create(nx_esrrf_batch** out, const nx_esrrf_item* items, int 
   for (auto& bi : b->items) {
     const nx_esrrf_plan* p = bi.desc.plan;
     const size_t planeM = (size_t)p->rowsM * p->colsM;
-    const int F = bi.mode == kModeFull ? 5 : 2 * bi.n_out;
+    const int F = bi.mode == kModeFull ? 5 : bi.n_out;
     bi.rec_off = off;
     off += align256((size_t)bi.n_tp * bi.chunks * F * planeM * sizeof(float));
     bi.mpc_off = off;
@@ -845,6 +875,16 @@ int nx_esrrf_batch_bind(nx_esrrf_batch* b, void* d_ws, size_t ws_bytes, void* st
   cudaStream_t s = (cudaStream_t)stream;
   char* base = (char*)d_ws;
   unsigned* status = (unsigned*)base;
+  while (b->side.size() + 1 < b->classes.size()) {
+    cudaStream_t st = nullptr;
+    NX_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    b->side.push_back(st);
+  }
+  while (b->events.size() < b->classes.size() + 1) {
+    cudaEvent_t e = nullptr;
+    NX_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    b->events.push_back(e);
+  }
   for (size_t c = 0; c < b->classes.size(); ++c) {
     auto& cl = b->classes[c];
     std::vector<FusedParams> params(cl.items.size());
@@ -858,7 +898,7 @@ int nx_esrrf_batch_bind(nx_esrrf_batch* b, void* d_ws, size_t ws_bytes, void* st
       if (bi.mode == kModeSum) {
         const int ns = bi.desc.n_sens > 0 ? bi.desc.n_sens : 1;
         fp.n_sens = ns;
-        fp.F = 2 * ns;
+        fp.F = ns;
         for (int k2 = 0; k2 < ns && bi.desc.n_sens > 0; ++k2) {
           const RgcScalars sc = rgc_scalars(p->M, p->radius, bi.desc.sens[k2], 0);
           fp.sens_mode_k[k2] = sc.sens_mode;
@@ -890,8 +930,17 @@ int nx_esrrf_batch_launch(const nx_esrrf_batch* b, void* stream) {
   char* base = (char*)b->d_ws;
   NX_CUDA_TRY(cudaMemsetAsync(base, 0, kStatusBytes + align256(b->classes.size() * sizeof(unsigned)),
                               s));
-  for (size_t c = 0; c < b->classes.size(); ++c) {
+  // class 0 runs on the caller's stream, class c > 0 on side stream c - 1,
+  // forked after the memset and joined back at the end: one class's wave tail,
+  // finalisation and macro-pixel correction overlap the next class's kernel
+  const size_t nc = b->classes.size();
+  if (nc > 1) {
+    NX_CUDA_TRY(cudaEventRecord(b->events[0], s));
+    for (size_t c = 1; c < nc; ++c) NX_CUDA_TRY(cudaStreamWaitEvent(b->side[c - 1], b->events[0], 0));
+  }
+  for (size_t c = 0; c < nc; ++c) {
     const auto& cl = b->classes[c];
+    cudaStream_t cs = c == 0 ? s : b->side[c - 1];
     UnitTable ut;
     memset(&ut, 0, sizeof(ut));
     ut.items = (const FusedParams*)(base + cl.params_off);
@@ -900,38 +949,40 @@ int nx_esrrf_batch_launch(const nx_esrrf_batch* b, void* stream) {
     ut.total_units = cl.unit_start.back();
     ut.counter = (unsigned*)(base + b->counters_off) + c;
     ut.ns_cap = cl.ns_cap;
-    cudaError_t e = cl.entry->launch[cl.mode](ut, cl.maps, cl.grid, s);
+    cudaError_t e = cl.entry->launch[cl.mode](ut, cl.maps, cl.grid, cs);
     if (e != cudaSuccess) return cuda_status(e, "batched eSRRF launch");
-  }
-  for (const auto& bi : b->items) {
-    const nx_esrrf_plan* p = bi.desc.plan;
-    const long long planeM = (long long)p->rowsM * p->colsM;
-    const bool full = bi.mode == kModeFull;
-    const int F = full ? 5 : 2 * bi.n_out;
-    const float* rec = (const float*)(base + bi.rec_off);
-    for (int tp = 0; tp < bi.n_tp; ++tp) {
-      const int nf = std::min(bi.fpt, bi.desc.T - tp * bi.fpt);
-      const int nch = std::min(bi.chunks, nf);
-      const float* rtp = rec + (size_t)tp * bi.chunks * F * planeM;
-      float* out = bi.desc.d_out + (size_t)tp * planeM;
-      const long long stride = (long long)bi.n_tp * planeM;
-      cudaError_t e;
-      if (full) {
-        e = launch_finalize(rtp, F, nch, nf, planeM, bi.desc.corr_mask, out, stride, true, s);
-      } else {
-        e = cudaSuccess;
-        for (int k = 0; k < bi.n_out && e == cudaSuccess; ++k)
-          e = launch_finalize(rtp + (size_t)2 * k * planeM, F, nch, nf, planeM, NX_CORR_AVG,
-                              out + (size_t)k * stride, stride, false, s);
+    for (int idx : cl.items) {
+      const auto& bi = b->items[idx];
+      const nx_esrrf_plan* p = bi.desc.plan;
+      const long long planeM = (long long)p->rowsM * p->colsM;
+      const bool full = bi.mode == kModeFull;
+      const int F = full ? 5 : bi.n_out;
+      const float* rec = (const float*)(base + bi.rec_off);
+      for (int tp = 0; tp < bi.n_tp; ++tp) {
+        const int nf = std::min(bi.fpt, bi.desc.T - tp * bi.fpt);
+        const int nch = std::min(bi.chunks, nf);
+        const float* rtp = rec + (size_t)tp * bi.chunks * F * planeM;
+        float* out = bi.desc.d_out + (size_t)tp * planeM;
+        const long long stride = (long long)bi.n_tp * planeM;
+        if (full) {
+          e = launch_finalize(rtp, F, nch, nf, planeM, bi.desc.corr_mask, out, stride, true, cs);
+        } else {
+          e = cudaSuccess;
+          for (int k = 0; k < bi.n_out && e == cudaSuccess; ++k)
+            e = launch_finalize(rtp + (size_t)k * planeM, F, nch, nf, planeM, NX_CORR_AVG,
+                                out + (size_t)k * stride, stride, false, cs);
+        }
+        if (e != cudaSuccess) return cuda_status(e, "batched temporal finalize");
       }
-      if (e != cudaSuccess) return cuda_status(e, "batched temporal finalize");
+      if (bi.desc.macro_pixel_correction) {
+        e = launch_mpc(bi.desc.d_out, bi.n_out * bi.n_tp, p->rowsM, p->colsM, p->M,
+                       (float*)(base + bi.mpc_off), cs);
+        if (e != cudaSuccess) return cuda_status(e, "batched macro-pixel correction");
+      }
     }
-    if (bi.desc.macro_pixel_correction) {
-      cudaError_t e = launch_mpc(bi.desc.d_out, bi.n_out * bi.n_tp, p->rowsM, p->colsM, p->M,
-                                 (float*)(base + bi.mpc_off), s);
-      if (e != cudaSuccess) return cuda_status(e, "batched macro-pixel correction");
-    }
+    if (c > 0) NX_CUDA_TRY(cudaEventRecord(b->events[c + 1], cs));
   }
+  for (size_t c = 1; c < nc; ++c) NX_CUDA_TRY(cudaStreamWaitEvent(s, b->events[c + 1], 0));
   return NX_OK;
 }
 
@@ -1038,6 +1089,72 @@ int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n, int o
   if (order > 4 || order < -1) return invalid("order must be -1, 0, 1, 2, 3 or 4");
   cudaError_t e = launch_srrf_temporal(d_stack, T, n, order, d_out, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_status(e, "SRRF temporal correlation");
+  return NX_OK;
+}
+
+}  // extern "C"
+
+namespace nx {
+
+// Loop control of the reference's ACRF with lag-time integration
+// (sr_temporal_correlations.py:159-200) replayed on the host in its own
+// arithmetic: the level count is a Python int (T) at the first level and a
+// float (T / order^k) after, compared with integer t; the binning of frame t
+// reads frames t*order .. t*order + order-2 when t*order < n_binned.
+static int acrf_schedule(int T, int order, AcrfSchedule* sch) {
+  memset(sch, 0, sizeof(*sch));
+  double nb = (double)T;
+  while (nb > (double)order) {
+    if (sch->n_levels >= kMaxAcrfLevels) return invalid("too many lag-time levels");
+    long long t = 0, n_bin = 0;
+    while ((double)t < nb - (double)order) {
+      if ((double)(t * order) < nb) {
+        if (t * order + order - 2 >= T) {
+          set_error("index %lld is out of bounds for axis 0 with size %d", t * order + order - 2,
+                    T);
+          return NX_ERR_INDEX;
+        }
+        n_bin = t + 1;
+      }
+      ++t;
+    }
+    const int L = sch->n_levels++;
+    sch->n_iter[L] = (int)t;
+    sch->n_bin[L] = (int)n_bin;
+    sch->n_binned[L] = (float)nb;
+    nb = nb / (double)order;
+  }
+  return NX_OK;
+}
+
+}  // namespace nx
+
+extern "C" {
+
+size_t nx_srrf_acrf_workspace_bytes(int T, long long n) {
+  if (T < 1 || n < 0) return 0;
+  return align256((size_t)T * (size_t)n * sizeof(float));
+}
+
+int nx_srrf_acrf_integrated(const float* d_stack, int T, long long n, int order, float* d_out,
+                            void* d_ws, size_t ws_bytes, void* stream) {
+  if (T < 1 || n < 0) return invalid("bad stack shape");
+  if (order < 2 || order > 4) return invalid("lag-time integration applies to orders 2, 3 and 4");
+  AcrfSchedule sch;
+  int rc = acrf_schedule(T, order, &sch);
+  if (rc) return rc;
+  if (n == 0) return NX_OK;
+  if (!d_stack || !d_out) return invalid("NULL stack/output");
+  if (!d_ws || ws_bytes < nx_srrf_acrf_workspace_bytes(T, n)) {
+    set_error("workspace too small: need %zu bytes", nx_srrf_acrf_workspace_bytes(T, n));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  float* im = (float*)d_ws;
+  NX_CUDA_TRY(cudaMemcpyAsync(im, d_stack, (size_t)T * n * sizeof(float), cudaMemcpyDeviceToDevice,
+                              s));
+  cudaError_t e = launch_srrf_acrf_integrated(im, T, n, order, sch, d_out, s);
+  if (e != cudaSuccess) return cuda_status(e, "ACRF with lag-time integration");
   return NX_OK;
 }
 

@@ -126,6 +126,71 @@ __host__ __device__ __forceinline__ int floordiv(int a, int b) {
   return (a % b != 0 && ((a < 0) != (b < 0))) ? q - 1 : q;
 }
 
+// ---------------------------------------------------------------------------
+// Streaming temporal moments of one pixel's time series x_0 .. x_{n-1} (float32).
+//
+//   mean   running mean (Welford: mean += (x - mean) / n)
+//   m2     sum_t (x_t - mean)^2
+//   c      sum_{t<n-1} (x_t - mean)(x_{t+1} - mean), the lag-1 co-moment about
+//          the CURRENT mean -- what TAC2 needs at the end
+//   a, b   x_{n-1} - mean and x_0 - mean (last and first value as deviations)
+//
+// Every update adds deviation-sized terms, so nothing cancels the way raw or
+// shifted power sums do.  Adding x as frame k (k >= 1 frames in, d = x - mean,
+// e = d / (k+1), mean' = mean + e): expanding the old pairs about mean' moves c
+// by e (a + b) + (k-1) e^2 (the centred values sum to zero) and the new pair
+// adds (a - e)(d - e); with k e^2 - e d = -e^2 this collapses to
+//   c' = c + a d + e (b - e),   m2' = m2 + d (d - e),   a' = d - e,   b' = b - e.
+// Two records of consecutive frames merge exactly with the pairwise formulas
+// of Chan, Golub and LeVeque plus the one pair that straddles the boundary.
+// AVG = mean, VAR = m2 / n, TAC2 = c / (n - 1)
+// (sr_temporal_correlations.py:46-75, 205-221).
+// ---------------------------------------------------------------------------
+struct Moments {
+  float mean, m2, c, a, b;
+};
+
+__host__ __device__ __forceinline__ Moments moments_start(float x) {
+  return Moments{x, 0.f, 0.f, 0.f, 0.f};
+}
+
+// x is frame k of the series (k >= 1 frames already folded in); inv = 1 / (k + 1)
+__device__ __forceinline__ void moments_push(Moments& s, float x, float inv) {
+  const float d = x - s.mean;
+  const float e = d * inv;
+  s.mean = s.mean + e;
+  const float bn = s.b - e;
+  s.c = fmaf(e, bn, fmaf(s.a, d, s.c));
+  const float u = d - e;
+  s.m2 = fmaf(d, u, s.m2);
+  s.a = u;
+  s.b = bn;
+}
+
+// a <- a (+) b where b's nb frames follow a's na frames (full: all fields,
+// else the mean only)
+__device__ __forceinline__ void moments_merge(Moments& a, const Moments& b, int na, int nb,
+                                              bool full) {
+  if (nb == 0) return;
+  if (na == 0) {
+    a = b;
+    return;
+  }
+  const float n = (float)na + (float)nb;
+  const float dl = b.mean - a.mean;
+  const float mn = fmaf(dl, __fdiv_rn((float)nb, n), a.mean);
+  if (full) {
+    const float da = mn - a.mean, db = mn - b.mean;
+    const float ca = a.c + da * (a.a + a.b) + (float)(na - 1) * (da * da);
+    const float cb = b.c + db * (b.a + b.b) + (float)(nb - 1) * (db * db);
+    a.c = ca + cb + (a.a - da) * (b.b - db);
+    a.m2 = a.m2 + b.m2 + (dl * dl) * __fdiv_rn((float)na * (float)nb, n);
+    a.a = b.a - db;
+    a.b = a.b - da;
+  }
+  a.mean = mn;
+}
+
 }  // namespace nx
 
 // host-side error plumbing shared by the C-ABI translation units

@@ -18,8 +18,9 @@
 //      on packed f32x2 arithmetic (both frames in one register pair);
 //   5. apply ^sensitivity, the intensity (column pass) and the margin, and
 //      either write the per-frame value (eSRRF_ST stack) or fold it into
-//      per-pixel temporal sums kept in shared memory (shift K = first value;
-//      S, Q, P, L).
+//      per-pixel streaming temporal moments kept in shared memory (Welford
+//      mean and M2, lag-1 co-moment, last and first value as deviations; see
+//      Moments).
 // Nothing of size (T, 2Hm, 2Wm) or (T, Hm, Wm) is ever materialised for the
 // temporal modes.
 #pragma once
@@ -35,7 +36,7 @@ namespace nx {
 enum FusedMode : int { kModeStack = 0, kModeSum = 1, kModeFull = 2 };
 
 __host__ __device__ constexpr int mode_fields(int mode) {
-  return mode == kModeFull ? 5 : (mode == kModeSum ? 2 : 0);
+  return mode == kModeFull ? 5 : (mode == kModeSum ? 1 : 0);
 }
 
 constexpr int kMaxSens = 4;    // sensitivities sharing one RGC pass (AVG mode)
@@ -60,11 +61,16 @@ struct FusedParams {
   unsigned* status;
   int tmap;              // index into the kernel's TMA descriptor pack, or -1: plain loads
   int tiles_y;
-  int F;                 // record fields: 5 (VAR/TAC2) or 2 * n_sens (AVG)
+  int F;                 // record fields: 5 (VAR/TAC2) or n_sens (AVG: the mean per sensitivity)
   int n_sens;            // AVG mode: sensitivities evaluated on the same RGC (others: 1)
   int sens_mode_k[kMaxSens];  // 0: none (s <= 1), 1: integer power sens_int_k, 2: powf(sens_k)
   int sens_int_k[kMaxSens];
   float sens_k[kMaxSens];
+  unsigned long long wait_ns;  // bound of every producer/consumer wait (0: kWaitLimitNs)
+  // failure-detection self-test only (0 in every computation): the producers
+  // withhold the `full` arrival of the first pass of each CTA's first unit, so
+  // the consumers' bounded wait runs out and the CTA takes its abort path
+  int test_withhold_full;
 };
 
 struct TmapPack {
@@ -182,14 +188,14 @@ struct Geo {
   static constexpr int O_CW = O_RW + S_RW;
   static constexpr int S_CW = al(OX * 5);
   // per-output temporal state kept out of registers, [px][consumer] planes:
-  //   FULL: float4 (K, S, Q, P) then float L;  SUM: float2 (K, S) per sensitivity
+  //   FULL: float4 (mean, M2, C, A) then float B;  SUM: the mean per sensitivity
   static constexpr int O_TW = O_CW + S_CW;     // 1 / sum w per output
   static constexpr int O_TK = O_TW + M * NTC;
   static constexpr int S_TK_FULL = 5 * M * NTC;
   static constexpr int O_BAR_FULL = O_TK + S_TK_FULL;
-  // AVG mode keeps K and S of ns_cap sensitivities per output
+  // AVG mode keeps the running mean of ns_cap sensitivities per output
   __host__ __device__ static constexpr int o_bar(int mode, int ns_cap) {
-    return mode == 1 ? O_TK + 2 * ns_cap * M * NTC : (mode == 2 ? O_BAR_FULL : O_TK);
+    return mode == 1 ? O_TK + ns_cap * M * NTC : (mode == 2 ? O_BAR_FULL : O_TK);
   }
   // 2 NSLOT + 1 + 2 FP (<= 11) mbarriers after o_bar
   __host__ __device__ static constexpr size_t smem_bytes(int mode, int ns_cap) {
@@ -473,7 +479,9 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
     for (int pp = 0; pp < NPR; ++pp)
 #pragma unroll
       for (int px = 0; px < M; ++px) acc2[pp][px] = make_float2(0.f, 0.f);
-#pragma unroll
+    // window rows stay a loop: unrolled, the core's code outgrows the
+    // instruction cache (measured 2 % slower and with register spills)
+#pragma unroll 1
     for (int jj = 0; jj < G::W2; ++jj) {
       const int kyl = 2 * ty + cpy + jj;
       const float4* r0 = hg + (kyl * 2 + 0) * G::HGP + lane;
@@ -606,6 +614,7 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
     cur_item = item;
   }
   const FusedParams& p = sp;
+  const unsigned long long lim = p.wait_ns ? p.wait_ns : kWaitLimitNs;
   const int local = unit - (ut.items ? __ldg(ut.unit_start + item) : 0);
   const int tiles = p.tiles_x * p.tiles_y;
   const int tile = local % tiles;
@@ -741,13 +750,13 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
       for (int fr = 0; fr < FP; ++fr)
         tin[fr] = prod.inb + (set * FP + (fr < nf ? fr : 0)) * G::S_INB;
       // slot s is free once the consumers released its previous use
-      bool ok = use == 0 || mbar_wait_or_abort(&empty[s], (use - 1) & 1u, &s_abort);
+      bool ok = use == 0 || mbar_wait_or_abort(&empty[s], (use - 1) & 1u, &s_abort, lim);
       if (ok && use_tma) {
 #pragma unroll
         for (int fr = 0; fr < FP; ++fr) {
           const int k = set * FP + fr;
           if (fr < nf && ok) {
-            ok = mbar_wait_or_abort(&tbar[k], (tphase >> k) & 1u, &s_abort);
+            ok = mbar_wait_or_abort(&tbar[k], (tphase >> k) & 1u, &s_abort, lim);
             if (ok) {
               tphase ^= 1u << k;
               tpend &= ~(1u << k);
@@ -766,7 +775,7 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
           }
         }
         mbar_arrive(pbar);
-        ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort);
+        ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort, lim);
         pphase ^= 1u;
       }
       if (!ok) {
@@ -775,7 +784,7 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
       }
       prod.roberts_and_rows(p, u, tin, s);
       mbar_arrive(pbar);
-      ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort);
+      ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort, lim);
       pphase ^= 1u;
       if (!ok) {
         *(volatile int*)&s_abort = 1;
@@ -797,14 +806,14 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
       }
       prod.column_pass(p, u);
       mbar_arrive(pbar);
-      ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort);
+      ok = mbar_wait_or_abort(pbar, pphase & 1u, &s_abort, lim);
       pphase ^= 1u;
       if (!ok) {
         *(volatile int*)&s_abort = 1;
         break;
       }
       prod.row_pass(p, u, s);
-      mbar_arrive(&full[s]);
+      if (!(p.test_withhold_full && iter == 0 && j == 0)) mbar_arrive(&full[s]);
     }
   } else {
     // ======================= consumers ======================================
@@ -815,7 +824,7 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
       const unsigned use = g / G::NSLOT;
       const int fa = f0 + j * FP;
       const int nf = min(FP, f1 - fa);
-      if (!mbar_wait_or_abort(&full[s], use & 1u, &s_abort)) {
+      if (!mbar_wait_or_abort(&full[s], use & 1u, &s_abort, lim)) {
         *(volatile int*)&s_abort = 1;
         break;
       }
@@ -835,6 +844,12 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
       }
       mbar_arrive(&empty[s]);  // slot s fully read
       const bool first = (fa == f0);
+      // frame fa + fr is frame k = fa - f0 + fr of this unit's series; 1 / (k + 1)
+      // by the fast reciprocal (the increment it scales is a deviation-sized term,
+      // so its ~1 ulp error does not show; the IEEE reciprocal cost 2 % of the kernel)
+      float inv_n[FP];
+#pragma unroll
+      for (int fr = 0; fr < FP; ++fr) inv_n[fr] = __fdividef(1.0f, (float)(fa - f0 + fr + 1));
 #pragma unroll
       for (int px = 0; px < M; ++px) {
         const float twv = tw[px * G::NTC + tid];
@@ -871,31 +886,21 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
         if (MODE == kModeSum) {
           // unrolled over the sensitivity slots (a runtime-bounded loop here
           // made the compiler re-materialise addresses in the RGC core: +14 %
-          // instructions)
+          // instructions); running mean per sensitivity (Welford)
 #pragma unroll
           for (int k = 0; k < kMaxSens; ++k) {
             if (k >= p.n_sens) break;
-            float2* ks = reinterpret_cast<float2*>(tk) + (k * M + px) * G::NTC + tid;
-            float kv = 0.f, sv = 0.f;
-            if (!first) {
-              const float2 t = *ks;
-              kv = t.x;
-              sv = t.y;
-            }
+            float* ks = tk + (k * M + px) * G::NTC + tid;
+            float mu = first ? 0.f : *ks;
 #pragma unroll
             for (int fr = 0; fr < FP; ++fr) {
               if (fr < nf) {
                 float r = apply_sens(base[fr], p.sens_mode_k[k], p.sens_int_k[k], p.sens_k[k]);
                 r = zero ? 0.f : r * ival[fr];
-                if (first && fr == 0) {
-                  kv = r;
-                  sv = 0.f;
-                } else {
-                  sv += r - kv;
-                }
+                mu = (first && fr == 0) ? r : fmaf(r - mu, inv_n[fr], mu);
               }
             }
-            *ks = make_float2(kv, sv);
+            *ks = mu;
           }
         } else if (MODE == kModeStack) {
 #pragma unroll
@@ -910,33 +915,22 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
         } else {
           float4* st = reinterpret_cast<float4*>(tk) + px * G::NTC + tid;
           float* stl = tk + 4 * M * G::NTC + px * G::NTC + tid;
-          float K = 0.f, S = 0.f, Q = 0.f, P = 0.f, L = 0.f;
+          Moments mo{0.f, 0.f, 0.f, 0.f, 0.f};
           if (!first) {
             const float4 t = *st;
-            K = t.x;
-            S = t.y;
-            Q = t.z;
-            P = t.w;
-            L = *stl;
+            mo = Moments{t.x, t.y, t.z, t.w, *stl};
           }
 #pragma unroll
           for (int fr = 0; fr < FP; ++fr) {
             if (fr < nf) {
               float r = apply_sens(base[fr], p.sens_mode_k[0], p.sens_int_k[0], p.sens_k[0]);
               r = zero ? 0.f : r * ival[fr];
-              if (first && fr == 0) {
-                K = r;
-              } else {
-                const float y = r - K;
-                S += y;
-                Q = fmaf(y, y, Q);
-                P = fmaf(L, y, P);
-                L = y;
-              }
+              if (first && fr == 0) mo = moments_start(r);
+              else moments_push(mo, r, inv_n[fr]);
             }
           }
-          *st = make_float4(K, S, Q, P);
-          *stl = L;
+          *st = make_float4(mo.mean, mo.m2, mo.c, mo.a);
+          *stl = mo.b;
         }
       }
     }
@@ -948,11 +942,7 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
     if (MODE == kModeSum) {
       for (int k = 0; k < p.n_sens; ++k) {
 #pragma unroll
-        for (int px = 0; px < M; ++px) {
-          const float2 t = reinterpret_cast<const float2*>(tk)[(k * M + px) * G::NTC + tid];
-          rec[(2 * k) * plane + px] = t.x;
-          rec[(2 * k + 1) * plane + px] = t.y;
-        }
+        for (int px = 0; px < M; ++px) rec[k * plane + px] = tk[(k * M + px) * G::NTC + tid];
       }
     } else {
 #pragma unroll

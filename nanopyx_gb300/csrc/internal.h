@@ -68,7 +68,7 @@ cudaError_t launch_srrf_fused(const float* in, const float* img_interp, int T, i
                               int M, const RingCoords& rc, float ring_radius, int border,
                               int positivity, int iw, float* out, cudaStream_t s);
 
-// temporal records: fields K, S, Q, P, L (planes of n_pixels)
+// temporal records: fields mean, M2, C, A, B of Moments (planes of n_pixels)
 cudaError_t launch_record_push_frame(const float* frame, long long n, float* rec, int it,
                                      cudaStream_t s);
 cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n_acc, int n_blk,
@@ -82,8 +82,23 @@ cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int co
                                   cudaStream_t s);
 cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int order, float* out,
                                  cudaStream_t s);
-// macro-pixel correction of S images in place; scratch holds S*M*M*kMpcChunks floats
+// ACRF with lag-time integration: per level, iterations over t, re-binned
+// frames (a prefix of t) and the divisor (float32 of the reference's count)
+constexpr int kMaxAcrfLevels = 48;
+struct AcrfSchedule {
+  int n_levels;
+  int n_iter[kMaxAcrfLevels];
+  int n_bin[kMaxAcrfLevels];
+  float n_binned[kMaxAcrfLevels];
+};
+// im: a (T, n) working copy of the stack, re-binned in place
+cudaError_t launch_srrf_acrf_integrated(float* im, int T, long long n, int order,
+                                        const AcrfSchedule& sch, float* out, cudaStream_t s);
+// macro-pixel correction of S images in place; the scratch it uses is
+// mpc_scratch_bytes(S, rowsM, M) = max(S,1) * M^2 * min(kMpcChunks, max(1, rowsM/M))
+// floats, never more than nx_macro_pixel_workspace_bytes(S, M)
 constexpr int kMpcChunks = 64;
+size_t mpc_scratch_bytes(int S, int rowsM, int M);
 cudaError_t launch_mpc(float* img, int S, int rowsM, int colsM, int M, float* map,
                        cudaStream_t s);
 

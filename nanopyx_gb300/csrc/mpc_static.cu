@@ -10,14 +10,22 @@
 // same correction with its scratch (the per-slice phase maps) in a fixed
 // device array owned by the library, so the caller passes only the images.
 //
-// * The array holds kStaticScratchBytes = 256 KiB and every GPU that loads this
-//   library keeps it until the process exits.  A call whose scratch would not
-//   fit (nx_macro_pixel_workspace_bytes(S, m) > 256 KiB) is rejected with
-//   NX_ERR_INVALID_ARG and a message naming the limit; nothing is launched.
+// * The array holds kStaticScratchBytes = 256 KiB.  A call needs
+//   max(S,1) * m^2 * min(64, max(1, rowsM / m)) floats of it (the per-slice,
+//   per-phase partial sums of the map); one that needs more is rejected with
+//   NX_ERR_INVALID_ARG and a message naming the limit, and nothing is launched.
+//   For images of at least 64 macro-pixel rows that is S * m^2 <= 1024.
 // * Host code cannot use the array's name as a device address.  The first call
 //   on each device looks the address up with cudaGetSymbolAddress (with that
-//   device current) and caches it; make that first call before any stream
-//   capture.
+//   device current) and caches it.  With lazy module loading (the default of
+//   CUDA 12.2 and later) that first call is also what loads this library's
+//   kernels on the device and reserves the array there, so it can fail with
+//   an out-of-memory error: make it once at start-up, before the phase that
+//   must not allocate and before any stream capture.  Under eager loading the
+//   array is reserved when the library's module loads.
+// * The cached address belongs to the device's context: do not use this entry
+//   point again after resetting that device (cudaDeviceReset) in the same
+//   process.
 // * All calls on a device share the array, which keeps the previous call's
 //   contents.  The map kernel writes every entry the apply kernel then reads,
 //   so nothing has to be cleared, but calls that overlap on the GPU (two
@@ -66,7 +74,7 @@ extern "C" int nx_macro_pixel_correct_static(float* d_img, int S, int rowsM, int
     nx::set_error("bad image shape or magnification");
     return NX_ERR_INVALID_ARG;
   }
-  const size_t need = nx_macro_pixel_workspace_bytes(S, magnification);
+  const size_t need = nx::mpc_scratch_bytes(S, rowsM, magnification);
   if (need > kStaticScratchBytes) {
     nx::set_error(
         "macro-pixel correction of %d slices at magnification %d needs %zu bytes of scratch; "

@@ -66,6 +66,99 @@ __global__ void cr_shift_magnify_kernel(const float* __restrict__ in, int T, int
   }
 }
 
+// Tiled form of the same resampling for magnifications >= 1: one CTA per
+// (frame, 32-row x 256-column output tile).  The sample coordinates and the
+// four Catmull-Rom weights of every output row and column of the tile are
+// computed once; the input patch the tile reads (zero outside the image, the
+// value the reference's skipped taps contribute) is staged in shared memory;
+// a vertical pass forms, for every output row and patch column, the 4-tap
+// column sum p the per-pixel kernel forms, and the horizontal pass adds the 4
+// column taps in the same order -- the same float operations as
+// cr_shift_magnify_kernel, so the same results, with 4 shared loads and one
+// coalesced store per output instead of 16 global loads and 20 weight
+// evaluations.
+constexpr int kCrTileRows = 32;
+constexpr int kCrTileCols = 256;
+constexpr int kCrPatchRows = kCrTileRows + 5;  // (rows - 1) / mag + 5 for mag >= 1
+constexpr int kCrPatchCols = kCrTileCols + 5;
+
+__global__ void __launch_bounds__(kCrTileCols)
+    cr_magnify_tiled_kernel(const float* __restrict__ in, int H, int W,
+                            const float* __restrict__ shift_r, const float* __restrict__ shift_c,
+                            float mag_r, float mag_c, int rowsM, int colsM,
+                            float* __restrict__ out) {
+  extern __shared__ float crs[];
+  float* patch = crs;                                  // [kCrPatchRows][kCrPatchCols]
+  float* P = patch + kCrPatchRows * kCrPatchCols;      // [kCrTileRows][kCrPatchCols]
+  float4* wr = reinterpret_cast<float4*>(P + kCrTileRows * kCrPatchCols);  // [kCrTileRows]
+  int* rbase = reinterpret_cast<int*>(wr + kCrTileRows);                   // [kCrTileRows]
+  const int t = blockIdx.z;
+  const int i0 = blockIdx.y * kCrTileRows;
+  const int j0 = blockIdx.x * kCrTileCols;
+  const float sr = shift_r[t], sc = shift_c[t];
+  const int tid = threadIdx.x;
+  // first patch row / column: the first tap of the tile's first output row / column
+  const float row0 = __fsub_rn(__fdiv_rn((float)i0, mag_r), sr);
+  const float col0 = __fsub_rn(__fdiv_rn((float)j0, mag_c), sc);
+  const int pr0 = (int)floorf(row0 - 0.5f) - 1;
+  const int pc0 = (int)floorf(col0 - 0.5f) - 1;
+  // this thread's output column: coordinate, validity, patch offset, weights
+  const int j = j0 + tid;
+  const float col = __fsub_rn(__fdiv_rn((float)j, mag_c), sc);
+  const bool cval = j < colsM && !(col < 0.f || col >= (float)W);
+  const int c_int = (int)floorf(col - 0.5f);
+  const int ci = c_int - 1 - pc0;
+  float wc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) wc[k] = cr_cubic(col - ((float)(c_int - 1 + k) + 0.5f));
+  if (tid < kCrTileRows) {
+    const int i = i0 + tid;
+    const float row = __fsub_rn(__fdiv_rn((float)i, mag_r), sr);
+    const int r_int = (int)floorf(row - 0.5f);
+    const bool rval = i < rowsM && !(row < 0.f || row >= (float)H);
+    float w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) w[k] = cr_cubic(row - ((float)(r_int - 1 + k) + 0.5f));
+    wr[tid] = make_float4(w[0], w[1], w[2], w[3]);
+    rbase[tid] = rval ? r_int - 1 - pr0 : -1;
+  }
+  const float* f = in + (size_t)t * H * W;
+  for (int idx = tid; idx < kCrPatchRows * kCrPatchCols; idx += kCrTileCols) {
+    const int r = pr0 + idx / kCrPatchCols, c = pc0 + idx % kCrPatchCols;
+    patch[idx] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(f + (size_t)r * W + c) : 0.f;
+  }
+  __syncthreads();
+  // vertical pass: P[i][c] = sum_l w_l(i) patch[rbase(i) + l][c] (fma order of
+  // the per-pixel kernel: l = 0..3)
+  for (int idx = tid; idx < kCrTileRows * kCrPatchCols; idx += kCrTileCols) {
+    const int il = idx / kCrPatchCols, c = idx % kCrPatchCols;
+    const int rb = rbase[il];
+    float p = 0.f;
+    if (rb >= 0) {
+      const float4 w = wr[il];
+      const float* pc = patch + rb * kCrPatchCols + c;
+      p = fmaf(pc[0], w.x, p);
+      p = fmaf(pc[kCrPatchCols], w.y, p);
+      p = fmaf(pc[2 * kCrPatchCols], w.z, p);
+      p = fmaf(pc[3 * kCrPatchCols], w.w, p);
+    }
+    P[idx] = p;
+  }
+  __syncthreads();
+  if (j >= colsM) return;
+  float* o = out + (size_t)t * rowsM * colsM + j;
+  const int iend = min(kCrTileRows, rowsM - i0);
+  for (int il = 0; il < iend; ++il) {
+    float q = 0.f;
+    if (cval && rbase[il] >= 0) {
+      const float* pp = P + il * kCrPatchCols + ci;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) q = fmaf(pp[k], wc[k], q);
+    }
+    o[(size_t)(i0 + il) * colsM] = q;
+  }
+}
+
 // _c_gradient_roberts_cross (src/include/_c_gradients.c:53-73), same
 // evaluation order, so bit-identical to the reference.
 __global__ void roberts_cross_kernel(const float* __restrict__ in, int T, int H, int W,
@@ -235,97 +328,68 @@ __global__ void radiality_kernel(const float* __restrict__ gx, const float* __re
 }
 
 // ---------------------------------------------------------------------------
-// temporal records  (K = first value, S = sum y, Q = sum y^2, P = sum y_t y_{t+1},
-// L = last y; y = x - K)
+// temporal records: planes mean, M2, C, A, B of Moments (common.cuh)
 // ---------------------------------------------------------------------------
 __global__ void record_push_frame_kernel(const float* __restrict__ frame, long long n,
                                          float* __restrict__ rec, int it) {
+  const float inv = __frcp_rn((float)(it + 1));
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const float v = frame[i];
-    if (it == 0) {
-      rec[i] = v;
-      rec[n + i] = 0.f;
-      rec[2 * n + i] = 0.f;
-      rec[3 * n + i] = 0.f;
-      rec[4 * n + i] = 0.f;
-    } else {
-      const float y = v - rec[i];
-      rec[n + i] += y;
-      rec[2 * n + i] = fmaf(y, y, rec[2 * n + i]);
-      rec[3 * n + i] = fmaf(rec[4 * n + i], y, rec[3 * n + i]);
-      rec[4 * n + i] = y;
+    Moments m = moments_start(v);
+    if (it > 0) {
+      m = Moments{rec[i], rec[n + i], rec[2 * n + i], rec[3 * n + i], rec[4 * n + i]};
+      moments_push(m, v, inv);
     }
+    rec[i] = m.mean;
+    rec[n + i] = m.m2;
+    rec[2 * n + i] = m.c;
+    rec[3 * n + i] = m.a;
+    rec[4 * n + i] = m.b;
   }
-}
-
-struct Rec {
-  float K, S, Q, P, L;
-};
-
-// A <- A (+) B where B's frames follow A's (associative merge of shifted sums)
-__device__ __forceinline__ void rec_merge(Rec& a, const Rec& b, int na, int nb, bool full) {
-  if (nb == 0) return;
-  if (na == 0) {
-    a = b;
-    return;
-  }
-  const float d = b.K - a.K;
-  const float fnb = (float)nb;
-  if (full) {
-    a.Q = a.Q + b.Q + 2.f * d * b.S + fnb * d * d;
-    a.P = a.P + b.P + d * (2.f * b.S - b.L) + (fnb - 1.f) * d * d + a.L * d;
-    a.L = b.L + d;
-  }
-  a.S = a.S + b.S + fnb * d;
 }
 
 __global__ void record_merge_kernel(float* __restrict__ acc, const float* __restrict__ blk,
                                     long long n, int na, int nb) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    Rec a{acc[i], acc[n + i], acc[2 * n + i], acc[3 * n + i], acc[4 * n + i]};
-    const Rec b{blk[i], blk[n + i], blk[2 * n + i], blk[3 * n + i], blk[4 * n + i]};
-    rec_merge(a, b, na, nb, true);
-    acc[i] = a.K;
-    acc[n + i] = a.S;
-    acc[2 * n + i] = a.Q;
-    acc[3 * n + i] = a.P;
-    acc[4 * n + i] = a.L;
+    Moments a{acc[i], acc[n + i], acc[2 * n + i], acc[3 * n + i], acc[4 * n + i]};
+    const Moments b{blk[i], blk[n + i], blk[2 * n + i], blk[3 * n + i], blk[4 * n + i]};
+    moments_merge(a, b, na, nb, true);
+    acc[i] = a.mean;
+    acc[n + i] = a.m2;
+    acc[2 * n + i] = a.c;
+    acc[3 * n + i] = a.a;
+    acc[4 * n + i] = a.b;
   }
 }
 
+// Merges the `nchunks` consecutive records of one timepoint in frame order and
+// writes the correlations of corr_mask.  full: 5-field records; else one field
+// (the mean) per record.
 __global__ void finalize_kernel(const float* __restrict__ rec, int F, int nchunks, int nf,
                                 long long n, int corr_mask, float* __restrict__ out,
                                 long long out_stride, bool full) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    Rec a{0.f, 0.f, 0.f, 0.f, 0.f};
+    Moments a{0.f, 0.f, 0.f, 0.f, 0.f};
     int na = 0;
     for (int c = 0; c < nchunks; ++c) {
       const int nc = (int)((long long)(c + 1) * nf / nchunks - (long long)c * nf / nchunks);
       const float* r = rec + (size_t)c * F * n;
-      Rec b{r[i], r[n + i], 0.f, 0.f, 0.f};
-      if (full) {
-        b.Q = r[2 * n + i];
-        b.P = r[3 * n + i];
-        b.L = r[4 * n + i];
-      }
-      rec_merge(a, b, na, nc, full);
+      Moments b{r[i], 0.f, 0.f, 0.f, 0.f};
+      if (full) b = Moments{r[i], r[n + i], r[2 * n + i], r[3 * n + i], r[4 * n + i]};
+      moments_merge(a, b, na, nc, full);
       na += nc;
     }
     const float fn = (float)na;
-    const float ybar = a.S / fn;
     int ci = 0;
-    if (corr_mask & NX_CORR_AVG) out[(ci++) * out_stride + i] = a.K + ybar;
+    if (corr_mask & NX_CORR_AVG) out[(ci++) * out_stride + i] = a.mean;
     if (corr_mask & NX_CORR_VAR) {
-      const float v = (a.Q - a.S * ybar) / fn;
+      const float v = __fdiv_rn(a.m2, fn);
       out[(ci++) * out_stride + i] = v > 0.f ? v : 0.f;
     }
-    if (corr_mask & NX_CORR_TAC2) {
-      const float num = a.P - ybar * (2.f * a.S - a.L) + (fn - 1.f) * ybar * ybar;
-      out[(ci++) * out_stride + i] = num / (fn - 1.f);
-    }
+    if (corr_mask & NX_CORR_TAC2) out[(ci++) * out_stride + i] = __fdiv_rn(a.c, fn - 1.f);
   }
 }
 
@@ -357,6 +421,46 @@ __global__ void temporal_stack_kernel(const float* __restrict__ x, int T, long l
       }
       out[i] = __fdiv_rn(q, (float)(T - 1));
     }
+  }
+}
+
+// The same correlations with each CTA's 128 pixels x T frames staged in
+// shared memory, so the stack is read from HBM once (the two-pass VAR / TAC2
+// of the per-pixel kernel read it twice); identical operations and order.
+constexpr int kTcPix = 128;
+constexpr int kTcMaxFrames = 400;  // 128 x 400 floats = 200 KB of shared memory
+
+__global__ void __launch_bounds__(kTcPix)
+    temporal_stack_smem_kernel(const float* __restrict__ x, int T, long long n, int corr,
+                               float* __restrict__ out) {
+  extern __shared__ float ts[];  // [T][kTcPix]
+  const long long p0 = (long long)blockIdx.x * kTcPix;
+  const int tid = threadIdx.x;
+  const long long i = p0 + tid;
+  const bool in = i < n;
+  for (int t = 0; t < T; ++t) ts[t * kTcPix + tid] = in ? __ldg(x + (size_t)t * n + i) : 0.f;
+  if (!in) return;  // each thread reads back only its own column
+  float s = 0.f;
+  for (int t = 0; t < T; ++t) s = __fadd_rn(s, ts[t * kTcPix + tid]);
+  const float mean = __fdiv_rn(s, (float)T);
+  if (corr == NX_CORR_AVG) {
+    out[i] = mean;
+  } else if (corr == NX_CORR_VAR) {
+    float q = 0.f;
+    for (int t = 0; t < T; ++t) {
+      const float c = __fsub_rn(ts[t * kTcPix + tid], mean);
+      q = __fadd_rn(q, __fmul_rn(c, c));
+    }
+    out[i] = __fdiv_rn(q, (float)T);
+  } else {
+    float q = 0.f;
+    float prev = __fsub_rn(ts[tid], mean);
+    for (int t = 1; t < T; ++t) {
+      const float c = __fsub_rn(ts[t * kTcPix + tid], mean);
+      q = __fadd_rn(q, __fmul_rn(prev, c));
+      prev = c;
+    }
+    out[i] = __fdiv_rn(q, (float)(T - 1));
   }
 }
 
@@ -416,6 +520,72 @@ __global__ void srrf_temporal_kernel(const float* __restrict__ x, int T, long lo
     else if (order == 4) v = fabsf(abcd - ab * cd - ac * bd - ad * bc);
     else v = fabsf(ab);
     out[i] = __fdiv_rn(v, (float)T);
+  }
+}
+
+// ACRF of order 2, 3, 4 with lag-time integration
+// (sr_temporal_correlations.py:111-121,159-200), one pixel per thread, the
+// reference's float32 operations in its order (no contraction).  Per level:
+// the lag products over t < n_iter (ab restarts, abc and the order-4 sums run
+// on across levels), and frame t, once read, is replaced in place by
+// sum_{k < order-1} frame[t*order + k] / order for t < n_bin (else 0) --
+// zeroed first, so the k = 0 term of t = 0 reads the zero.  The last level's
+// correlation over n_binned is the result; 0 when no level runs.
+__global__ void srrf_acrf_integrated_kernel(float* __restrict__ im, int T, long long n, int order,
+                                            AcrfSchedule sch, float* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    float* x = im + i;
+    float s = 0.f;
+    for (int t = 0; t < T; ++t) s = __fadd_rn(s, x[(size_t)t * n]);
+    const float mean = __fdiv_rn(s, (float)T);
+    const float fo = (float)order;
+    float res = 0.f;
+    float abc = 0.f, abcd = 0.f, cd = 0.f, ac = 0.f, bd = 0.f, ad = 0.f, bc = 0.f;
+    for (int L = 0; L < sch.n_levels; ++L) {
+      float ab = 0.f;
+      const int n_iter = sch.n_iter[L], n_bin = sch.n_bin[L];
+      for (int t = 0; t < n_iter; ++t) {
+        const float a = __fsub_rn(x[(size_t)t * n], mean);
+        const float b = __fsub_rn(x[(size_t)(t + 1) * n], mean);
+        const float pab = __fmul_rn(a, b);
+        ab = __fadd_rn(ab, pab);
+        if (order == 3) {
+          const float c = __fsub_rn(x[(size_t)(t + 2) * n], mean);
+          abc = __fadd_rn(__fadd_rn(abc, pab), c);
+        } else if (order == 4) {
+          const float c = __fsub_rn(x[(size_t)(t + 2) * n], mean);
+          const float d = __fsub_rn(x[(size_t)(t + 3) * n], mean);
+          abcd = __fadd_rn(abcd, __fmul_rn(__fmul_rn(pab, c), d));
+          cd = __fadd_rn(cd, __fmul_rn(c, d));
+          ac = __fadd_rn(ac, __fmul_rn(a, c));
+          bd = __fadd_rn(bd, __fmul_rn(b, d));
+          ad = __fadd_rn(ad, __fmul_rn(a, d));
+          bc = __fadd_rn(bc, __fmul_rn(b, c));
+        }
+        float v = 0.f;
+        if (t < n_bin) {
+          const int tb = t * order;
+          for (int k = 0; k < order - 1; ++k) {
+            const float src = (tb + k == t) ? v : x[(size_t)(tb + k) * n];
+            v = __fadd_rn(v, __fdiv_rn(src, fo));
+          }
+        }
+        x[(size_t)t * n] = v;
+      }
+      float num;
+      if (order == 3) {
+        num = fabsf(abc);
+      } else if (order == 4) {
+        num = __fsub_rn(__fsub_rn(__fsub_rn(abcd, __fmul_rn(ab, cd)), __fmul_rn(ac, bd)),
+                        __fmul_rn(ad, bc));
+        num = fabsf(num);
+      } else {
+        num = fabsf(ab);
+      }
+      res = __fdiv_rn(num, sch.n_binned[L]);
+    }
+    out[i] = res;
   }
 }
 
@@ -498,6 +668,25 @@ cudaError_t launch_cr_shift_magnify(const float* in, int T, int H, int W, const 
                                     int colsM, float* out, cudaStream_t s) {
   const long long n = (long long)T * rowsM * colsM;
   if (n == 0) return cudaSuccess;
+  if (mag_r >= 1.f && mag_c >= 1.f && T <= 65535 && rowsM / kCrTileRows < 65535) {
+    static const size_t smem = (size_t)(kCrPatchRows + kCrTileRows) * kCrPatchCols * sizeof(float) +
+                               kCrTileRows * (sizeof(float4) + sizeof(int));
+    static int attr_dev = -1;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (attr_dev != dev) {
+      e = cudaFuncSetAttribute(cr_magnify_tiled_kernel,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      attr_dev = dev;
+    }
+    const dim3 grid((unsigned)((colsM + kCrTileCols - 1) / kCrTileCols),
+                    (unsigned)((rowsM + kCrTileRows - 1) / kCrTileRows), (unsigned)T);
+    cr_magnify_tiled_kernel<<<grid, kCrTileCols, smem, s>>>(in, H, W, shift_r, shift_c, mag_r,
+                                                            mag_c, rowsM, colsM, out);
+    return cudaGetLastError();
+  }
   cr_shift_magnify_kernel<<<grid_for(n), kBlock, 0, s>>>(in, T, H, W, shift_r, shift_c, mag_r,
                                                          mag_c, rowsM, colsM, out);
   return cudaGetLastError();
@@ -598,6 +787,23 @@ cudaError_t launch_finalize(const float* rec, int F, int nchunks, int nf, long l
 cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int corr, float* out,
                                   cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  const long long blocks = (n + kTcPix - 1) / kTcPix;
+  if (T >= 1 && T <= kTcMaxFrames && blocks <= 0x7fffffffLL) {
+    static int attr_dev = -1;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (attr_dev != dev) {
+      e = cudaFuncSetAttribute(temporal_stack_smem_kernel,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(kTcMaxFrames * kTcPix * sizeof(float)));
+      if (e != cudaSuccess) return e;
+      attr_dev = dev;
+    }
+    temporal_stack_smem_kernel<<<(unsigned)blocks, kTcPix, (size_t)T * kTcPix * sizeof(float),
+                                 s>>>(stack, T, n, corr, out);
+    return cudaGetLastError();
+  }
   temporal_stack_kernel<<<grid_for(n), kBlock, 0, s>>>(stack, T, n, corr, out);
   return cudaGetLastError();
 }
@@ -609,11 +815,25 @@ cudaError_t launch_srrf_temporal(const float* stack, int T, long long n, int ord
   return cudaGetLastError();
 }
 
+cudaError_t launch_srrf_acrf_integrated(float* im, int T, long long n, int order,
+                                        const AcrfSchedule& sch, float* out, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  srrf_acrf_integrated_kernel<<<grid_for(n), kBlock, 0, s>>>(im, T, n, order, sch, out);
+  return cudaGetLastError();
+}
+
+// partial-sum chunks of the macro-pixel map per (slice, phase row)
+static int mpc_chunks(int rowsM, int M) { return std::max(1, std::min(kMpcChunks, rowsM / M)); }
+
+size_t mpc_scratch_bytes(int S, int rowsM, int M) {
+  return (size_t)std::max(S, 1) * M * M * mpc_chunks(rowsM, M) * sizeof(float);
+}
+
 cudaError_t launch_mpc(float* img, int S, int rowsM, int colsM, int M, float* map,
                        cudaStream_t s) {
   if ((long long)S * rowsM * colsM == 0) return cudaSuccess;
   const int rows = rowsM / M;
-  const int nch = std::max(1, std::min(kMpcChunks, rows));
+  const int nch = mpc_chunks(rowsM, M);
   const int block = M <= 32 ? 32 * M : ((1024 / M) * M);
   if (rows > 0) {
     mpc_partial_kernel<<<dim3((unsigned)S, (unsigned)M, (unsigned)nch), block,

@@ -32,7 +32,7 @@ import torch
 from . import _native as N
 from ._device import check_image, get_plan, require_cuda, workspace
 
-__all__ = ["EsrrfBatch", "esrrf_batch", "sweep_batch", "tune_frames_per_unit"]
+__all__ = ["EsrrfBatch", "SweepGrid", "esrrf_batch", "sweep_batch", "tune_frames_per_unit"]
 
 _CACHE_PATH = os.path.join(os.path.expanduser("~"), ".cache", "nanopyx_gb300", "autotune.json")
 _cache_lock = threading.Lock()
@@ -195,32 +195,52 @@ def esrrf_batch(stacks, params, graph: bool = False):
     return b.run(graph=graph)
 
 
+class SweepGrid:
+    """The (sensitivity x radius) AVG reconstruction grid of one stack, planned
+    once and run as often as needed (``run(graph=True)`` replays one CUDA graph).
+
+    One batch item per radius and group of up to four sensitivities: the RGC
+    map of a radius is evaluated once per frame and raised to each sensitivity
+    in the epilogue.  ``run`` returns a device tensor
+    (len(sensitivities), len(radii), n_tp, H*m, W*m).
+    """
+
+    def __init__(self, stack, magnification: int, sensitivities, radii,
+                 frames_per_timepoint: int = 0, doIntensityWeighting: bool = True,
+                 macro_pixel_correction: bool = False, frames_per_unit: int = 0):
+        self.batch = b = EsrrfBatch()
+        t = stack if isinstance(stack, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(check_image(stack)))
+        t = check_image(t).to(b.device).contiguous()
+        self.sens, self.radii = list(sensitivities), list(radii)
+        self.groups = [self.sens[i:i + 4] for i in range(0, len(self.sens), 4)]
+        self.index = {}
+        for r in self.radii:
+            for g in self.groups:
+                self.index[(float(r), tuple(g))] = b.add(
+                    t, magnification, r, list(g), frames_per_timepoint, "AVG",
+                    doIntensityWeighting, macro_pixel_correction, frames_per_unit)
+        b.plan()
+
+    def run(self, graph: bool = False, check: bool = True):
+        outs = self.batch.run(graph=graph, check=check)
+        rows = []
+        for si in range(len(self.sens)):
+            g = self.groups[si // 4]
+            rows.append(torch.stack([outs[self.index[(float(r), tuple(g))]][si % 4]
+                                     for r in self.radii]))
+        return torch.stack(rows)
+
+
 def sweep_batch(stack, magnification: int, sensitivities, radii, frames_per_timepoint: int = 0,
                 doIntensityWeighting: bool = True, macro_pixel_correction: bool = False,
                 graph: bool = False):
-    """The (sensitivity x radius) AVG reconstruction grid in one batch.
-
-    Returns a device tensor (len(sensitivities), len(radii), n_tp, H*m, W*m).
+    """The (sensitivity x radius) AVG reconstruction grid in one batch (see
+    ``SweepGrid``).  Returns a device tensor
+    (len(sensitivities), len(radii), n_tp, H*m, W*m).
     """
-    b = EsrrfBatch()
-    t = stack if isinstance(stack, torch.Tensor) else torch.from_numpy(
-        np.ascontiguousarray(check_image(stack)))
-    t = check_image(t).to(b.device).contiguous()
-    sens = list(sensitivities)
-    groups = [sens[i:i + 4] for i in range(0, len(sens), 4)]
-    index = {}
-    for r in radii:
-        for g in groups:
-            index[(float(r), tuple(g))] = b.add(t, magnification, r, list(g),
-                                                frames_per_timepoint, "AVG",
-                                                doIntensityWeighting, macro_pixel_correction)
-    outs = b.run(graph=graph)
-    rows = []
-    for si, s in enumerate(sens):
-        g = groups[si // 4]
-        k = si % 4
-        rows.append(torch.stack([outs[index[(float(r), tuple(g))]][k] for r in radii]))
-    return torch.stack(rows)
+    return SweepGrid(stack, magnification, sensitivities, radii, frames_per_timepoint,
+                     doIntensityWeighting, macro_pixel_correction).run(graph=graph)
 
 
 # ---------------------------------------------------------------------------

@@ -317,8 +317,9 @@ def run_esrrf_parameter_sweep(*args, **kwargs):
 class ESRRFAccumulator:
     """Device-resident temporal state of one eSRRF reconstruction.
 
-    Frame blocks are pushed as they arrive (``push``); the per-pixel shifted
-    sums (K, S, Q, P, L) stay on the device between pushes, so a reconstruction
+    Frame blocks are pushed as they arrive (``push``); the per-pixel streaming
+    moments (first value, running mean, M2, lag-1 co-moment, last value) stay
+    on the device between pushes, so a reconstruction
     over many blocks never holds its per-frame stack anywhere.  ``finalize``
     returns the requested correlations (each (H*m, W*m)), macro-pixel corrected
     if asked, with the same arithmetic as ``eSRRF`` over one timepoint.

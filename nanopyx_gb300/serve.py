@@ -14,8 +14,9 @@ runs a dispatcher thread that
 * finalises a request after its last block (temporal correlation + macro-pixel
   correction on the device) and copies the result back asynchronously.
 
-Latency is measured from the arrival of a request's last block to its result
-being on the host.  ``serve_plain`` is the plain per-request path the server is
+Two latencies are kept per request: from the arrival of its last block to its
+result being on the host (``latency``), and from the arrival of its first
+block (``first_latency``).  ``serve_plain`` is the plain per-request path the server is
 compared with: one request at a time, every call synchronous.
 
 There is no reference counterpart: NanoPyx keeps a whole per-frame stack in
@@ -57,6 +58,7 @@ class Request:
         self.iw = bool(doIntensityWeighting)
         self.single = isinstance(temporal_correlation, str)
         self.t_submit = time.perf_counter()
+        self.t_first_block = None
         self.t_last_block = None
         self.t_done = None
         self.host_blocks = collections.deque()
@@ -80,7 +82,13 @@ class Request:
 
     @property
     def latency(self):
+        """Seconds from the arrival of the last block to the result on the host."""
         return None if self.t_done is None else self.t_done - self.t_last_block
+
+    @property
+    def first_latency(self):
+        """Seconds from the arrival of the first block to the result on the host."""
+        return None if self.t_done is None else self.t_done - self.t_first_block
 
     def result(self, timeout=None):
         if not self._done.wait(timeout):
@@ -150,6 +158,8 @@ class ESRRFServer:
             if req.blocks_received >= req.n_blocks:
                 raise ValueError("request already received all its blocks")
             req.host_blocks.append(a)
+            if req.blocks_received == 0:
+                req.t_first_block = time.perf_counter()
             req.blocks_received += 1
             req.mpx_frames += a.shape[0] * req.H * req.W / 1e6
             if req.blocks_received == req.n_blocks:

@@ -247,17 +247,25 @@ def calculate_eSRRF_temporal_correlations(im, correlation: str):
 
 
 def calculate_SRRF_temporal_correlations(im, order: int = 1, do_integrate_lag_times: bool = 0):
-    """Orders 0 (max), 1 (mean), -1 (pairwise product sum), 2/3/4 (ACRF)."""
+    """Orders 0 (max), 1 (mean), -1 (pairwise product sum), 2/3/4 (ACRF, with
+    or without lag-time integration; the flag only applies to orders 2-4, as in
+    sr_temporal_correlations.py:31-41,111-202).  Raises IndexError at the frame
+    counts where the reference's lag-time binning indexes past its input."""
     st = _stack3(im)
     assert order <= 4
-    if do_integrate_lag_times and order not in (0, 1, -1):
-        raise NotImplementedError("ACRF with lag-time integration is not implemented")
     if order < -1:
         raise ValueError("order must be -1, 0, 1, 2, 3 or 4")
     T = st.shape[0]
     out = torch.empty(st.shape[1:], dtype=torch.float32, device=st.t.device)
-    N.check(N.lib().nx_srrf_temporal_correlation(st.ptr(), T, out.numel(), int(order), _ptr(out),
-                                                 stream_ptr()),
+    L = N.lib()
+    if do_integrate_lag_times == 1 and order >= 2:
+        ws = workspace(L.nx_srrf_acrf_workspace_bytes(T, out.numel()), st.t.device)
+        N.check(L.nx_srrf_acrf_integrated(st.ptr(), T, out.numel(), int(order), _ptr(out),
+                                          _ptr(ws), ws.numel(), stream_ptr()),
+                "ACRF with lag-time integration")
+        return st.out(out)
+    N.check(L.nx_srrf_temporal_correlation(st.ptr(), T, out.numel(), int(order), _ptr(out),
+                                           stream_ptr()),
             "SRRF temporal correlation")
     return st.out(out)
 

@@ -72,7 +72,8 @@ def test_frames_per_unit_does_not_change_the_result_beyond_rounding():
         b = engine.EsrrfBatch()
         b.add(x, 5, 1.5, 2, 0, ("VAR", "TAC2"), frames_per_unit=fpu)
         outs.append(b.run()[0].cpu().numpy())
-    # different frame chunkings only reorder float32 sums (TAC2 has the most
-    # cancellation); both stay far inside the 1e-4 parity bar
-    assert rel_err(outs[0][0], outs[1][0]) <= 5e-5
-    assert rel_err(outs[0][1], outs[1][1]) <= 5e-5
+    # different frame chunkings only change the float32 rounding of the
+    # streamed moments (Welford updates within a chunk, pairwise merges across
+    # chunks), which stays at the level of a few float32 ulps of the deviations
+    assert rel_err(outs[0][0], outs[1][0]) <= 1e-5
+    assert rel_err(outs[0][1], outs[1][1]) <= 1e-5

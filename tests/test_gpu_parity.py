@@ -66,6 +66,31 @@ def test_shift_magnify_matches_reference(golden):
     assert rel_err(op.run(x, 0, 0, 10, 10), golden["cr/2"]) <= 1e-6
 
 
+@pytest.mark.parametrize("mag_r,mag_c,sr,sc", [(0.5, 0.75, 0.0, 0.0), (2.5, 3.0, 0.3, -1.2),
+                                               (1.0, 7.0, -2.0, 0.5), (5.0, 5.0, 0.0, 0.0)])
+def test_shift_magnify_tiles_and_small_magnifications_against_oracle(mag_r, mag_c, sr, sc):
+    """Magnifications >= 1 run the tiled kernel (partial tiles at these sizes),
+    smaller ones the per-pixel kernel; both against the FP64 oracle."""
+    x = blinking_stack(3, 37, 70, 12, seed=61)
+    got = nx.CRShiftAndMagnify(verbose=False).run(x, sr, sc, mag_r, mag_c)
+    ref = O.cr_shift_magnify(x, sr, sc, mag_r, mag_c)
+    assert got.shape == ref.shape
+    # the oracle's sampling coordinates are float64, the reference's (and these)
+    # float32 i / mag - shift
+    assert rel_err(got, ref) <= 1e-5
+
+
+def test_temporal_correlations_long_stacks_against_oracle():
+    """T <= 400 stages each pixel block in shared memory, longer stacks use the
+    two-pass per-pixel kernel; both against float64."""
+    rng = np.random.default_rng(62)
+    for T in (3, 400, 401):
+        x = (rng.random((T, 9, 13)) * 3 + 0.5).astype(np.float32)
+        for corr in ("AVG", "VAR", "TAC2"):
+            got = nx.calculate_eSRRF_temporal_correlations(x, corr)
+            assert rel_err(got, O.temporal_correlation(x, corr)) <= 1e-5, (T, corr)
+
+
 def test_roberts_cross_bit_exact(golden):
     gc, gr = nx.GradientRobertsCross(verbose=False).run(golden["cr/input"])
     assert np.array_equal(gc, golden["robx/gc"])
@@ -105,6 +130,28 @@ def test_temporal_correlations_match_numpy_reference(golden):
     for order in (0, 1, -1, 2, 3, 4):
         got = nx.calculate_SRRF_temporal_correlations(xs, order)
         assert rel_err(got, golden[f"srrf_temporal/{order}"]) <= 1e-5, order
+
+
+@pytest.mark.parametrize("T,order", [(12, 2), (12, 3), (12, 4), (39, 3), (40, 2), (40, 4)])
+def test_acrf_lag_integration_matches_reference(golden, T, order):
+    x = golden[f"srrf_lag/{T}/input"]
+    got = nx.calculate_SRRF_temporal_correlations(x, order, True)
+    assert rel_err(got, golden[f"srrf_lag/{T}/{order}"]) <= 1e-6
+    # the input is not modified (the re-binning works on a copy)
+    assert np.array_equal(x, golden[f"srrf_lag/{T}/input"])
+
+
+def test_acrf_lag_integration_larger_stack_and_index_errors():
+    x = blinking_stack(100, 40, 48, 10, seed=51)
+    for order in (2, 4):
+        got = nx.calculate_SRRF_temporal_correlations(x, order, True)
+        assert rel_err(got, O.srrf_acrf_integrated(x, order)) <= 1e-5, order
+    for T, order in ((7, 3), (9, 4)):
+        with pytest.raises(IndexError):
+            nx.calculate_SRRF_temporal_correlations(x[:T], order, True)
+    # the flag does not apply to orders 0, 1, -1 (as in the reference)
+    assert np.array_equal(nx.calculate_SRRF_temporal_correlations(x, 1, True),
+                          nx.calculate_SRRF_temporal_correlations(x, 1))
 
 
 def test_macro_pixel_corrector_matches_reference(golden):

@@ -102,3 +102,15 @@ def test_argument_checks_run_before_any_device_work(lib):
     assert lib.nx_macro_pixel_correct_static(P(256), 100000, 10, 10, 5, None) == \
         _native.NX_ERR_INVALID_ARG
     assert b"static scratch" in lib.nx_last_error()
+    # fused-kernel abort self-test: a plan is required before anything runs
+    assert lib.nx_selftest_fused_abort(None, None, 1, None, None, 0, 20_000_000, None) == \
+        _native.NX_ERR_INVALID_ARG
+    # ACRF with lag-time integration: bad order, and the reference's IndexError
+    # frame counts, are rejected on the host
+    assert lib.nx_srrf_acrf_integrated(None, 12, 10, 5, None, None, 0, None) == \
+        _native.NX_ERR_INVALID_ARG
+    assert lib.nx_srrf_acrf_integrated(None, 7, 10, 3, None, None, 0, None) == \
+        _native.NX_ERR_INDEX
+    assert b"out of bounds" in lib.nx_last_error()
+    assert lib.nx_srrf_acrf_integrated(None, 12, 10, 3, None, None, 0, None) == \
+        _native.NX_ERR_INVALID_ARG
