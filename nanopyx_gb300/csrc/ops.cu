@@ -87,11 +87,13 @@ __global__ void __launch_bounds__(kCrTileCols)
                             const float* __restrict__ shift_r, const float* __restrict__ shift_c,
                             float mag_r, float mag_c, int rowsM, int colsM,
                             float* __restrict__ out) {
-  extern __shared__ float crs[];
-  float* patch = crs;                                  // [kCrPatchRows][kCrPatchCols]
-  float* P = patch + kCrPatchRows * kCrPatchCols;      // [kCrTileRows][kCrPatchCols]
-  float4* wr = reinterpret_cast<float4*>(P + kCrTileRows * kCrPatchCols);  // [kCrTileRows]
-  int* rbase = reinterpret_cast<int*>(wr + kCrTileRows);                   // [kCrTileRows]
+  // the float4 row weights first, at the 16-byte aligned base (behind the
+  // patch and P they would start at byte 72036, which is not 16-byte aligned)
+  extern __shared__ __align__(16) float crs[];
+  float4* wr = reinterpret_cast<float4*>(crs);                  // [kCrTileRows]
+  int* rbase = reinterpret_cast<int*>(wr + kCrTileRows);        // [kCrTileRows]
+  float* patch = reinterpret_cast<float*>(rbase + kCrTileRows); // [kCrPatchRows][kCrPatchCols]
+  float* P = patch + kCrPatchRows * kCrPatchCols;               // [kCrTileRows][kCrPatchCols]
   const int t = blockIdx.z;
   const int i0 = blockIdx.y * kCrTileRows;
   const int j0 = blockIdx.x * kCrTileCols;
