@@ -439,7 +439,7 @@ def run_gpu_arm(args):
                                 for r, x in zip(rates, sweep)]
         line["served"] = sweep[-1]
         torch.cuda.empty_cache()
-        line["srrf"] = bench_srrf(dev, stack_np)
+        line["srrf"] = bench_srrf(dev, stack_np, peak=peak)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = time_cpu_baseline(stack_np)
     print(json.dumps(line), flush=True)
@@ -651,55 +651,100 @@ def served_blocks(sizes, seed=11, density=0.006):
             for H in sizes}
 
 
-def bench_srrf(dev, stack_np, frames=20, repeats=2):
-    """SRRF (ring 0.5, 12 ring points, m=5) + order-1 temporal mean on the 512 x 512 stack."""
+def srrf_flops(T, H, W, m):
+    """FLOP = sum_frames H W m^2 (12 (2 * 32 + 12) + 20): 12 ring points, two
+    16-tap Catmull-Rom interpolations of the gradient (32 FLOP each) and ~12
+    FLOP of radiality per point, plus ~20 per output for the intensity and
+    normalisation."""
+    return T * H * W * m * m * (12.0 * (2 * 32 + 12) + 20.0)
+
+
+def bench_srrf(dev, stack_np, frames=None, fpt=100, peak=None):
+    """SRRF (ring 0.5, 12 ring points, m=5) + per-frame macro-pixel correction
+    on the stack, then the order-1 temporal mean per 100-frame timepoint -- the
+    reference's SRRF() followed by calculate_SRRF_temporal_correlations, one
+    timepoint block at a time on the device."""
     import torch
 
     import nanopyx_gb300 as nx
+    from nanopyx_gb300 import _native as N
+    from nanopyx_gb300._device import workspace
 
-    x = torch.from_numpy(np.ascontiguousarray(stack_np[:frames])).to(dev)
+    T = stack_np.shape[0] if frames is None else frames
+    H, W = stack_np.shape[1:]
+    m = 5
+    x = torch.from_numpy(np.ascontiguousarray(stack_np[:T])).to(dev)
+    blocks = [(a, min(T, a + fpt)) for a in range(0, T, fpt)]
 
     def one():
-        rad = nx.SRRF(x, magnification=5, ringRadius=0.5)
-        return nx.calculate_SRRF_temporal_correlations(rad, 1)
+        return [nx.calculate_SRRF_temporal_correlations(
+            nx.SRRF(x[a:b], magnification=m, ringRadius=0.5), 1) for a, b in blocks]
 
     one()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(repeats):
-        one()
+    one()
     torch.cuda.synchronize(dev)
-    dt = (time.perf_counter() - t0) / repeats
-    res = {"workload": f"SRRF {frames}x512x512, m=5, ring 0.5 (12 points), MPC, order-1 mean",
-           "value": frames * 512 * 512 / 1e6 / dt, "unit": "Mpx*frames/s", "seconds": dt}
+    dt = time.perf_counter() - t0
+    res = {"workload": f"SRRF {T}x{H}x{W}, m={m}, ring 0.5 (12 points), per-frame MPC, "
+                       f"order-1 mean per {fpt}-frame timepoint (device-resident input)",
+           "value": T * H * W / 1e6 / dt, "unit": "Mpx*frames/s", "seconds": dt}
+    # the fused radiality kernel alone, per timepoint block (CUDA events)
+    L = N.lib()
+    s = torch.cuda.current_stream(dev)
+    nb = max(b - a for a, b in blocks)
+    out = torch.empty((nb, H * m, W * m), dtype=torch.float32, device=dev)
+    ws = workspace(L.nx_radiality_workspace_bytes(nb, H, W), dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in blocks]
+    for (a, b), (e0, e1) in zip(blocks, ev):
+        e0.record(s)
+        N.check(L.nx_radiality(x[a:b].data_ptr(), None, b - a, H, W, m, 0.5, 0, 1, 1,
+                               out.data_ptr(), ws.data_ptr(), ws.numel(), s.cuda_stream),
+                "radiality")
+        e1.record(s)
+    torch.cuda.synchronize(dev)
+    kern_ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
+    flops = srrf_flops(T, H, W, m)
+    achieved = flops / (kern_ms * 1e-3) / 1e12
+    res["roofline"] = {"bound": "fp32", "kernel": "srrf_fused_kernel<5>", "kernel_ms": kern_ms,
+                       "flops": flops, "achieved": achieved, "unit": "TFLOP/s",
+                       "peak": peak, "frac": (achieved / peak) if peak else None}
+    del out, ws
     if cpu_reference_available():
         from oracle import ref_build
 
         R = ref_build.load()
-        smp = np.ascontiguousarray(stack_np[:2])
-        mag = R["CRShiftAndMagnify"](verbose=False).run(smp, 0, 0, 5, 5, run_type="Threaded")
+        smp = np.ascontiguousarray(stack_np[:4])
+        R["Radiality"](verbose=False).run(smp[:1], R["CRShiftAndMagnify"](verbose=False).run(
+            smp[:1], 0, 0, m, m, run_type="Threaded"), magnification=m, ringRadius=0.5,
+            run_type="Threaded")  # warm-up
         t0 = time.perf_counter()
-        rad = R["Radiality"](verbose=False).run(smp, mag, magnification=5, ringRadius=0.5,
+        mag = R["CRShiftAndMagnify"](verbose=False).run(smp, 0, 0, m, m, run_type="Threaded")
+        rad = R["Radiality"](verbose=False).run(smp, mag, magnification=m, ringRadius=0.5,
                                                 run_type="Threaded")
-        R["macro_pixel_corrector"](rad, magnification=5)
+        R["calculate_SRRF_temporal_correlations"](R["macro_pixel_corrector"](
+            rad, magnification=m), 1)
         cdt = time.perf_counter() - t0
-        res["cpu_reference"] = {"value": 2 * 512 * 512 / 1e6 / cdt, "cores": os.cpu_count(),
-                                "sample": "2 frames, compiled reference Radiality(Threaded) + "
-                                          "macro_pixel_corrector (magnified input precomputed)"}
+        res["cpu_baseline"] = {"value": 4 * H * W / 1e6 / cdt, "unit": "Mpx*frames/s",
+                               "cores": os.cpu_count(), "kind": "reference",
+                               "sample": "4 frames as one timepoint: compiled reference "
+                                         "CRShiftAndMagnify + Radiality (Threaded) + "
+                                         "macro_pixel_corrector + order-1 mean"}
     return res
 
 
-def bench_standalone_ops(dev):
+def bench_standalone_ops(dev, T=100):
     """HBM throughput of the standalone ops off the fused path: Catmull-Rom
-    ShiftAndMagnify (100 x 512 x 512, m=5) and the eSRRF temporal correlations
-    of a 100 x 2560 x 2560 stack, against the measured HBM copy bandwidth."""
+    ShiftAndMagnify (T x 512 x 512, m=5) and the eSRRF temporal correlations
+    of a T x 2560 x 2560 stack, against the measured HBM copy bandwidth."""
     import torch
 
     from nanopyx_gb300 import _native as N
 
     L = N.lib()
     s = torch.cuda.current_stream(dev)
-    T, H, W, m = 100, 512, 512, 5
+    H, W, m = 512, 512, 5
     x = torch.rand((T, H, W), device=dev)
     zr = torch.zeros(T, device=dev)
     out = torch.empty((T, H * m, W * m), device=dev)
@@ -727,12 +772,12 @@ def bench_standalone_ops(dev):
         x.data_ptr(), T, H, W, zr.data_ptr(), zr.data_ptr(), 5.0, 5.0, out.data_ptr(),
         s.cuda_stream), "cr"))
     b = (x.numel() + out.numel()) * 4
-    rows.append({"op": "cr_shift_magnify 100x512x512 m=5", "ms": ms, "gbs": b / ms / 1e6})
+    rows.append({"op": f"cr_shift_magnify {T}x512x512 m=5", "ms": ms, "gbs": b / ms / 1e6})
     for name, c in (("AVG", 1), ("VAR", 2), ("TAC2", 4)):
         ms = timeit(lambda: N.check(L.nx_temporal_correlation(
             stack.data_ptr(), T, H * m * W * m, c, res.data_ptr(), s.cuda_stream), "tc"))
         b = (stack.numel() + res.numel()) * 4
-        rows.append({"op": f"temporal {name} 100x2560x2560", "ms": ms, "gbs": b / ms / 1e6})
+        rows.append({"op": f"temporal {name} {T}x2560x2560", "ms": ms, "gbs": b / ms / 1e6})
     for r in rows:
         r["frac_of_measured_hbm"] = r["gbs"] / peak
     return {"hbm_peak_gbs": peak, "ops": rows}
@@ -747,10 +792,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--srrf-only", action="store_true",
                     help="only the SRRF measurement (profiling the radiality kernel)")
-    ap.add_argument("--srrf-frames", type=int, default=20)
+    ap.add_argument("--srrf-frames", type=int, default=100)
     ap.add_argument("--ops-only", action="store_true",
                     help="only the HBM throughput of the standalone ShiftAndMagnify and "
                          "temporal-correlation kernels")
+    ap.add_argument("--ops-frames", type=int, default=100,
+                    help="frames of the standalone-op measurement")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the uneven-batch, sweep and served-stream measurements")
     ap.add_argument("--served-requests", type=int, default=200,
@@ -768,7 +815,8 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps(bench_standalone_ops(torch.device("cuda", 0))), flush=True)
+        print(json.dumps(bench_standalone_ops(torch.device("cuda", 0), T=args.ops_frames)),
+              flush=True)
         return 0
     if args.srrf_only:
         import torch
@@ -777,8 +825,9 @@ def main():
 
         torch.cuda.set_device(0)
         st = blinking_stack(args.srrf_frames, CFG["H"], CFG["W"], CFG["emitters"], seed=CFG["seed"])
-        print(json.dumps(bench_srrf(torch.device("cuda", 0), st, frames=args.srrf_frames)),
-              flush=True)
+        dev = torch.device("cuda", 0)
+        peak = max(measure_fp32_peak(dev), measure_fp32_peak(dev, packed=True))
+        print(json.dumps(bench_srrf(dev, st, frames=args.srrf_frames, peak=peak)), flush=True)
         return 0
     return run_gpu_arm(args)
 

@@ -40,11 +40,18 @@ struct SrrfTile {
   static constexpr int O_RW = O_RI + al(OY * RIW);      // intensity row weights [OY][5]
   static constexpr int O_CW = O_RW + al(OY * 5);        // intensity col weights [OX][5]
   static constexpr int O_RT = O_CW + al(OX * 5);        // ring row taps [OY][12][8]
-  // ring col taps: float4 halves [ring][px][2][lane] (lane-contiguous, conflict-free)
-  static constexpr int O_CT = O_RT + al(OY * kRing * 8);
-  // per-warp row pass of the gradient interpolation: [warp][ring][IW] float2
-  static constexpr int O_RB = O_CT + al(OX * kRing * 8);
-  static constexpr int FLOATS = O_RB + (NT / 32) * kRing * IW * 2;
+  // ring column taps of output column (lane, px) as 5 weights on the columns
+  // cb .. cb + 4 of the row-pass buffer, cb = the first tap of px = 0 (the taps
+  // of px = 1 .. M-1 start at cb or cb + 1): [ring][px][lane] float4 (weights
+  // 0..3) and float (weight 4), lane-contiguous
+  static constexpr int O_CW4 = O_RT + al(OY * kRing * 8);
+  static constexpr int O_CW1 = O_CW4 + al(kRing * M * TX * 4);
+  static constexpr int O_CB = O_CW1 + al(kRing * M * TX);  // [ring][lane] int: cb - x_start
+  // per-warp row pass of the gradient interpolation: [warp][ring][IW] float2,
+  // plus one zeroed float2 after the last ring (read with weight 0)
+  static constexpr int RBW = kRing * IW * 2 + 2;
+  static constexpr int O_RB = O_CB + al(kRing * TX);
+  static constexpr int FLOATS = O_RB + (NT / 32) * RBW;
   static constexpr size_t SMEM = size_t(FLOATS) * 4;
 };
 
@@ -86,8 +93,10 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
   float* rw = sm + G::O_RW;
   float* cw = sm + G::O_CW;
   float* rt = sm + G::O_RT;
-  float* ct = sm + G::O_CT;
-  float2* rb = reinterpret_cast<float2*>(sm + G::O_RB) + (threadIdx.x >> 5) * kRing * G::IW;
+  float4* cw4 = reinterpret_cast<float4*>(sm + G::O_CW4);
+  float* cw1 = sm + G::O_CW1;
+  int* cbt = reinterpret_cast<int*>(sm + G::O_CB);
+  float2* rb = reinterpret_cast<float2*>(sm + G::O_RB + (threadIdx.x >> 5) * G::RBW);
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -137,16 +146,30 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
     }
 #pragma unroll
     for (int k = 0; k < 5; ++k) cw[i * 5 + k] = w5[k];
-    const float xc = (float)xM + 0.5f;
-    const int ln = i / M, pxi = i % M;
-    for (int s = 0; s < kRing; ++s) {
-      float e[8];
-      ring_entry(e, xc, p.xr[s], M, w);
-      float4* dst = reinterpret_cast<float4*>(ct) + ((s * M + pxi) * 2) * 32 + ln;
-      dst[0] = make_float4(e[0], e[1], e[2], e[3]);
-      dst[32] = make_float4(e[4], e[5], e[6], e[7]);
-    }
   }
+  for (int i = tid; i < kRing * G::TX; i += G::NT) {
+    const int s = i / G::TX, ln = i % G::TX;
+    int cb = 0;
+    for (int px = 0; px < M; ++px) {
+      float e[8];
+      ring_entry(e, (float)((nx0 + ln) * M + px) + 0.5f, p.xr[s], M, w);
+      const int c0 = __float_as_int(e[0]);
+      if (px == 0) cb = c0;
+      // 0 or 1: the M phases of one lane span less than one input pixel
+      const int off = min(max(c0 - cb, 0), 1);
+      // a column outside the image contributes nothing (the reference skips
+      // it): all its weights are zero
+      float w5[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (e[6] != 0.f) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) w5[u + off] = e[1 + u];
+      }
+      cw4[(s * M + px) * G::TX + ln] = make_float4(w5[0], w5[1], w5[2], w5[3]);
+      cw1[(s * M + px) * G::TX + ln] = w5[4];
+    }
+    cbt[s * G::TX + ln] = cb - x_start;
+  }
+  if ((tid & 31) == 0) rb[kRing * G::IW] = make_float2(0.f, 0.f);
 
   const int ny = ny0 + ty, nx = nx0 + lane;
   const int j = ny * M + py;  // output row
@@ -211,43 +234,52 @@ __global__ void __launch_bounds__(SrrfTile<M>::NT, 1) srrf_fused_kernel(const Sr
       rb[idx] = v;
     }
     __syncwarp();
-    // radiality of this thread's M outputs
-#pragma unroll 1
+    // radiality of this thread's M outputs, ring point by ring point: the M
+    // columns share one window of 5 row-pass columns (cb .. cb + 4), each
+    // output weights it with its own 5-vector (its 4 taps and a zero), which
+    // is the 4-tap fma sequence of the reference with a + 0 at one end
+    float div[M];
+#pragma unroll
+    for (int px = 0; px < M; ++px) div[px] = 0.f;
+    const float yc = (float)j + 0.5f;
+#pragma unroll 2
+    for (int s = 0; s < kRing; ++s) {
+      const float dy = __fsub_rn(yc, __fadd_rn(yc, p.yr[s]));  // yc - y0
+      const float2* rp = rb + s * G::IW + cbt[s * G::TX + lane];
+      float2 col[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) col[k] = rp[k];
+#pragma unroll
+      for (int px = 0; px < M; ++px) {
+        const float4 wa = cw4[(s * M + px) * G::TX + lane];
+        const float we = cw1[(s * M + px) * G::TX + lane];
+        const float wv[5] = {wa.x, wa.y, wa.z, wa.w, we};
+        const float xc = (float)(nx * M + px) + 0.5f;
+        const float dx = __fsub_rn(xc, __fadd_rn(xc, p.xr[s]));  // xc - x0
+        float vgx = 0.f, vgy = 0.f;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+          vgx = fmaf(col[k].x, wv[k], vgx);
+          vgy = fmaf(col[k].y, wv[k], vgy);
+        }
+        float dk = 0.f;
+        const float g2 = vgx * vgx + vgy * vgy;
+        if (g2 != 0.f) {
+          // |vGy (xc - x0) - vGx (yc - y0)| / GMag / ringRadius
+          dk = 1.f - fabsf(vgy * dx - vgx * dy) * rsqrtf(g2) * p.inv_rr;
+          dk = dk * dk;
+        }
+        if (vgx * p.xr[s] + vgy * p.yr[s] > 0.f) div[px] -= dk;
+        else div[px] += dk;
+      }
+    }
+#pragma unroll
     for (int px = 0; px < M; ++px) {
       const int i = nx * M + px;  // output column
       float val = 0.f;
       if (row_ok && nx < w && i >= lo_i && i < hi_i) {
-        const float4* crow = reinterpret_cast<const float4*>(ct) + (px * 2) * 32 + lane;
-        float div = 0.f;
-#pragma unroll  // all 12 ring points in flight (measured 4.5 % faster than 4)
-        for (int s = 0; s < kRing; ++s) {
-          const float4 rB = *reinterpret_cast<const float4*>(rrow + s * 8 + 4);
-          const float4 cA = crow[(s * M * 2) * 32];
-          const float4 cB = crow[(s * M * 2 + 1) * 32];
-          float dk = 0.f;
-          float vgx = 0.f, vgy = 0.f;
-          if (rB.z != 0.f && cB.z != 0.f) {
-            const int c0 = __float_as_int(cA.x) - x_start;
-            const float wc[4] = {cA.y, cA.z, cA.w, cB.x};
-            const float2* rp = rb + s * G::IW + c0;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const float2 a = rp[u];
-              vgx = fmaf(a.x, wc[u], vgx);
-              vgy = fmaf(a.y, wc[u], vgy);
-            }
-            const float g2 = vgx * vgx + vgy * vgy;
-            if (g2 != 0.f) {
-              // |vGy (xc - x0) - vGx (yc - y0)| / GMag / ringRadius
-              dk = 1.f - fabsf(vgy * cB.y - vgx * rB.y) * rsqrtf(g2) * p.inv_rr;
-              dk = dk * dk;
-            }
-          }
-          if (vgx * p.xr[s] + vgy * p.yr[s] > 0.f) div -= dk;
-          else div += dk;
-        }
-        div /= 12.f;
-        val = p.positivity ? fmaxf(div, 0.f) : div;
+        const float dv = div[px] / 12.f;
+        val = p.positivity ? fmaxf(dv, 0.f) : dv;
         if (p.iw) {
           if (own_intensity) {
             // column pass of the intensity magnification (5 taps of the row pass)
