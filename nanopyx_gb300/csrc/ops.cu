@@ -79,21 +79,26 @@ __global__ void cr_shift_magnify_kernel(const float* __restrict__ in, int T, int
 // evaluations.
 constexpr int kCrTileRows = 32;
 constexpr int kCrTileCols = 256;
-constexpr int kCrPatchRows = kCrTileRows + 5;  // (rows - 1) / mag + 5 for mag >= 1
-constexpr int kCrPatchCols = kCrTileCols + 5;
+
+// Patch rows / columns a tile can touch at magnification mag >= 1: the taps of
+// n consecutive outputs start within floor((n - 1) / mag) + 1 input pixels of
+// each other (the extra 1 covers the float rounding of i / mag - shift), plus
+// the 4 taps, plus one spare.
+inline int cr_patch_extent(int n_out, float mag) {
+  return (int)std::floor((double)(n_out - 1) / (double)mag) + 6;
+}
 
 __global__ void __launch_bounds__(kCrTileCols)
     cr_magnify_tiled_kernel(const float* __restrict__ in, int H, int W,
                             const float* __restrict__ shift_r, const float* __restrict__ shift_c,
-                            float mag_r, float mag_c, int rowsM, int colsM,
+                            float mag_r, float mag_c, int rowsM, int colsM, int PR, int PC,
                             float* __restrict__ out) {
-  // the float4 row weights first, at the 16-byte aligned base (behind the
-  // patch and P they would start at byte 72036, which is not 16-byte aligned)
+  // the float4 row weights first, at the 16-byte aligned base
   extern __shared__ __align__(16) float crs[];
   float4* wr = reinterpret_cast<float4*>(crs);                  // [kCrTileRows]
   int* rbase = reinterpret_cast<int*>(wr + kCrTileRows);        // [kCrTileRows]
-  float* patch = reinterpret_cast<float*>(rbase + kCrTileRows); // [kCrPatchRows][kCrPatchCols]
-  float* P = patch + kCrPatchRows * kCrPatchCols;               // [kCrTileRows][kCrPatchCols]
+  float* patch = reinterpret_cast<float*>(rbase + kCrTileRows); // [PR][PC]
+  float* P = patch + PR * PC;                                   // [kCrTileRows][PC]
   const int t = blockIdx.z;
   const int i0 = blockIdx.y * kCrTileRows;
   const int j0 = blockIdx.x * kCrTileCols;
@@ -107,9 +112,9 @@ __global__ void __launch_bounds__(kCrTileCols)
   // this thread's output column: coordinate, validity, patch offset, weights
   const int j = j0 + tid;
   const float col = __fsub_rn(__fdiv_rn((float)j, mag_c), sc);
-  const bool cval = j < colsM && !(col < 0.f || col >= (float)W);
   const int c_int = (int)floorf(col - 0.5f);
   const int ci = c_int - 1 - pc0;
+  const bool cval = j < colsM && !(col < 0.f || col >= (float)W) && ci >= 0 && ci + 3 < PC;
   float wc[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) wc[k] = cr_cubic(col - ((float)(c_int - 1 + k) + 0.5f));
@@ -117,32 +122,33 @@ __global__ void __launch_bounds__(kCrTileCols)
     const int i = i0 + tid;
     const float row = __fsub_rn(__fdiv_rn((float)i, mag_r), sr);
     const int r_int = (int)floorf(row - 0.5f);
-    const bool rval = i < rowsM && !(row < 0.f || row >= (float)H);
+    const int rb = r_int - 1 - pr0;
+    const bool rval = i < rowsM && !(row < 0.f || row >= (float)H) && rb >= 0 && rb + 3 < PR;
     float w[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) w[k] = cr_cubic(row - ((float)(r_int - 1 + k) + 0.5f));
     wr[tid] = make_float4(w[0], w[1], w[2], w[3]);
-    rbase[tid] = rval ? r_int - 1 - pr0 : -1;
+    rbase[tid] = rval ? rb : -1;
   }
   const float* f = in + (size_t)t * H * W;
-  for (int idx = tid; idx < kCrPatchRows * kCrPatchCols; idx += kCrTileCols) {
-    const int r = pr0 + idx / kCrPatchCols, c = pc0 + idx % kCrPatchCols;
+  for (int idx = tid; idx < PR * PC; idx += kCrTileCols) {
+    const int r = pr0 + idx / PC, c = pc0 + idx % PC;
     patch[idx] = (r >= 0 && r < H && c >= 0 && c < W) ? __ldg(f + (size_t)r * W + c) : 0.f;
   }
   __syncthreads();
   // vertical pass: P[i][c] = sum_l w_l(i) patch[rbase(i) + l][c] (fma order of
   // the per-pixel kernel: l = 0..3)
-  for (int idx = tid; idx < kCrTileRows * kCrPatchCols; idx += kCrTileCols) {
-    const int il = idx / kCrPatchCols, c = idx % kCrPatchCols;
+  for (int idx = tid; idx < kCrTileRows * PC; idx += kCrTileCols) {
+    const int il = idx / PC, c = idx % PC;
     const int rb = rbase[il];
     float p = 0.f;
     if (rb >= 0) {
       const float4 w = wr[il];
-      const float* pc = patch + rb * kCrPatchCols + c;
+      const float* pc = patch + rb * PC + c;
       p = fmaf(pc[0], w.x, p);
-      p = fmaf(pc[kCrPatchCols], w.y, p);
-      p = fmaf(pc[2 * kCrPatchCols], w.z, p);
-      p = fmaf(pc[3 * kCrPatchCols], w.w, p);
+      p = fmaf(pc[PC], w.y, p);
+      p = fmaf(pc[2 * PC], w.z, p);
+      p = fmaf(pc[3 * PC], w.w, p);
     }
     P[idx] = p;
   }
@@ -153,7 +159,7 @@ __global__ void __launch_bounds__(kCrTileCols)
   for (int il = 0; il < iend; ++il) {
     float q = 0.f;
     if (cval && rbase[il] >= 0) {
-      const float* pp = P + il * kCrPatchCols + ci;
+      const float* pp = P + il * PC + ci;
 #pragma unroll
       for (int k = 0; k < 4; ++k) q = fmaf(pp[k], wc[k], q);
     }
@@ -426,21 +432,34 @@ __global__ void temporal_stack_kernel(const float* __restrict__ x, int T, long l
   }
 }
 
-// The same correlations with each CTA's 128 pixels x T frames staged in
-// shared memory, so the stack is read from HBM once (the two-pass VAR / TAC2
-// of the per-pixel kernel read it twice); identical operations and order.
+// VAR and TAC2 with each CTA's 128 pixels x T frames staged in shared memory,
+// so the stack is read from HBM once (the two-pass per-pixel kernel reads it
+// twice); identical operations and order.
 constexpr int kTcPix = 128;
 constexpr int kTcMaxFrames = 400;  // 128 x 400 floats = 200 KB of shared memory
 
 __global__ void __launch_bounds__(kTcPix)
     temporal_stack_smem_kernel(const float* __restrict__ x, int T, long long n, int corr,
-                               float* __restrict__ out) {
-  extern __shared__ float ts[];  // [T][kTcPix]
+                               bool vec, float* __restrict__ out) {
+  extern __shared__ __align__(16) float ts[];  // [T][kTcPix]
   const long long p0 = (long long)blockIdx.x * kTcPix;
   const int tid = threadIdx.x;
   const long long i = p0 + tid;
   const bool in = i < n;
-  for (int t = 0; t < T; ++t) ts[t * kTcPix + tid] = in ? __ldg(x + (size_t)t * n + i) : 0.f;
+  if (vec) {
+    // every 16-byte piece of the CTA's T x 128 block as one asynchronous copy,
+    // all issued before the single wait (enough bytes in flight to fill HBM)
+    for (int k = tid; k < T * (kTcPix / 4); k += kTcPix) {
+      const int t = k / (kTcPix / 4), c = (k % (kTcPix / 4)) * 4;
+      const unsigned dst = smem_addr(ts + t * kTcPix + c);
+      const float* src = x + (size_t)t * n + p0 + c;
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+  } else {
+    for (int t = 0; t < T; ++t) ts[t * kTcPix + tid] = in ? __ldg(x + (size_t)t * n + i) : 0.f;
+  }
   if (!in) return;  // each thread reads back only its own column
   float s = 0.f;
   for (int t = 0; t < T; ++t) s = __fadd_rn(s, ts[t * kTcPix + tid]);
@@ -671,22 +690,29 @@ cudaError_t launch_cr_shift_magnify(const float* in, int T, int H, int W, const 
   const long long n = (long long)T * rowsM * colsM;
   if (n == 0) return cudaSuccess;
   if (mag_r >= 1.f && mag_c >= 1.f && T <= 65535 && rowsM / kCrTileRows < 65535) {
-    static const size_t smem = (size_t)(kCrPatchRows + kCrTileRows) * kCrPatchCols * sizeof(float) +
-                               kCrTileRows * (sizeof(float4) + sizeof(int));
+    // shared memory for the largest patch (magnification 1); each launch uses
+    // the extent its magnifications need
+    static const size_t smem_max =
+        (size_t)(cr_patch_extent(kCrTileRows, 1.f) + kCrTileRows) *
+            cr_patch_extent(kCrTileCols, 1.f) * sizeof(float) +
+        kCrTileRows * (sizeof(float4) + sizeof(int));
     static int attr_dev = -1;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (attr_dev != dev) {
       e = cudaFuncSetAttribute(cr_magnify_tiled_kernel,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
       if (e != cudaSuccess) return e;
       attr_dev = dev;
     }
+    const int PR = cr_patch_extent(kCrTileRows, mag_r), PC = cr_patch_extent(kCrTileCols, mag_c);
+    const size_t smem = (size_t)(PR + kCrTileRows) * PC * sizeof(float) +
+                        kCrTileRows * (sizeof(float4) + sizeof(int));
     const dim3 grid((unsigned)((colsM + kCrTileCols - 1) / kCrTileCols),
                     (unsigned)((rowsM + kCrTileRows - 1) / kCrTileRows), (unsigned)T);
     cr_magnify_tiled_kernel<<<grid, kCrTileCols, smem, s>>>(in, H, W, shift_r, shift_c, mag_r,
-                                                            mag_c, rowsM, colsM, out);
+                                                            mag_c, rowsM, colsM, PR, PC, out);
     return cudaGetLastError();
   }
   cr_shift_magnify_kernel<<<grid_for(n), kBlock, 0, s>>>(in, T, H, W, shift_r, shift_c, mag_r,
@@ -790,7 +816,12 @@ cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int co
                                   cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   const long long blocks = (n + kTcPix - 1) / kTcPix;
-  if (T >= 1 && T <= kTcMaxFrames && blocks <= 0x7fffffffLL) {
+  // AVG reads the stack once in the per-pixel kernel already; VAR and TAC2
+  // re-read it there, so they stage each pixel block in shared memory
+  if (corr != NX_CORR_AVG && T >= 1 && T <= kTcMaxFrames && blocks <= 0x7fffffffLL) {
+    // 16-byte copies need a 16-byte aligned base, whole 4-pixel pieces in every
+    // frame (n % 4 == 0) and a whole last block
+    const bool vec = (reinterpret_cast<uintptr_t>(stack) & 15u) == 0 && n % kTcPix == 0;
     static int attr_dev = -1;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -803,7 +834,7 @@ cudaError_t launch_temporal_stack(const float* stack, int T, long long n, int co
       attr_dev = dev;
     }
     temporal_stack_smem_kernel<<<(unsigned)blocks, kTcPix, (size_t)T * kTcPix * sizeof(float),
-                                 s>>>(stack, T, n, corr, out);
+                                 s>>>(stack, T, n, corr, vec, out);
     return cudaGetLastError();
   }
   temporal_stack_kernel<<<grid_for(n), kBlock, 0, s>>>(stack, T, n, corr, out);
