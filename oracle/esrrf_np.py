@@ -24,6 +24,10 @@ inside the reference project):
   integration, ``sr_temporal_correlations.py:111-121,159-200``.
 * ``macro_pixel_correct``  -- ``src/nanopyx/core/transform/mpcorrector.pyx:26-73``.
 * ``esrrf``  -- ``src/nanopyx/methods/esrrf/eSRRF_workflow.py:58-121``.
+* ``mirror_square`` / ``fht_interpolate_frame`` / ``fht_space_interpolation`` /
+  ``esrrf_st_fht``  -- the use_fht=True path,
+  ``src/nanopyx/core/transform/interpolation.py:22-290`` and
+  ``_le_esrrf.pyx:183-188``.
 * ``gradient_radiality`` / ``radiality`` / ``srrf``  --
   ``src/include/_c_gradients.c:3-25``, ``src/include/_c_sr_radiality.c:6-51``,
   ``src/nanopyx/core/transform/_le_radiality.pyx:86-125`` and
@@ -283,6 +287,113 @@ def esrrf_st(stack, magnification=5, radius=1.5, sensitivity=1, doIntensityWeigh
                        rowsM, colsM, m, p, margin)
         out[t] = f * mag if doIntensityWeighting else f
     return out
+
+
+# ----------------------------------------------------------------------------
+# FHT (Fourier) interpolation, the use_fht=True path of eSRRF_ST
+# (src/nanopyx/core/transform/interpolation.py:22-290, _le_esrrf.pyx:183-188)
+# ----------------------------------------------------------------------------
+def _pow2_ceil(n):
+    return 1 if n <= 1 else 1 << int(np.ceil(np.log2(n)))
+
+
+def mirror_square(img):
+    """The frame tiled with alternating mirror images (an odd number of copies
+    per axis, the centre copy upright) and cropped centrally to the smallest
+    power-of-two square covering both sides (interpolation.py:22-55)."""
+    h, w = img.shape
+    n = max(_pow2_ceil(h), _pow2_ceil(w))
+    copies = []
+    for dim, axis_len in ((0, h), (1, w)):
+        k = -(-n // axis_len)
+        k += 1 - k % 2                       # odd
+        mid = (k - 1) // 2
+        idx = np.concatenate([np.arange(axis_len) if (c - mid) % 2 == 0
+                              else np.arange(axis_len)[::-1] for c in range(k)])
+        start = (k * axis_len - n) // 2
+        copies.append(idx[start:start + n])
+    return img[np.ix_(copies[0], copies[1])]
+
+
+def fht_interpolate_frame(img, mag):
+    """Zero-padded-spectrum interpolation of one frame (interpolation.py:58-111):
+    the mirrored square's spectrum (real FFT along x, full along y) is moved
+    into a mag-times larger zero spectrum (the y frequencies at or above half
+    the size go to the top end), inverted, rescaled onto the frame's own
+    [min, max] and cropped to the frame's magnified extent.  float64."""
+    img = np.asarray(img, dtype=np.float64)
+    lo, hi = float(np.float32(img.min())), float(np.float32(img.max()))
+    sq = mirror_square(img)
+    n = sq.shape[0]
+    L = n * mag
+    spec = np.fft.rfft2(sq)
+    big = np.zeros((L, L // 2 + 1), dtype=np.complex128)
+    keep = (n + 1) // 2
+    big[:keep, :spec.shape[1]] = spec[:keep]
+    big[L - (n - keep):, :spec.shape[1]] = spec[keep:]
+    z = np.fft.irfft2(big, s=(L, L))
+    zlo, zhi = z.min(), z.max()
+    if zhi != zlo:
+        z = (z - zlo) * ((hi - lo) / (zhi - zlo)) + lo
+    y0 = (L - mag * img.shape[0]) // 2
+    x0 = (L - mag * img.shape[1]) // 2
+    return z[y0:y0 + mag * img.shape[0], x0:x0 + mag * img.shape[1]]
+
+
+def _tile_starts(dim, ts, step):
+    s = list(range(0, dim, step))
+    if s and s[-1] + ts < dim:
+        s.append(max(0, dim - ts))
+    return s
+
+
+def fht_space_interpolation(stack, mag, tile=256, overlap=16):
+    """Per frame: frames up to `tile` pixels a side in one piece; larger ones in
+    overlapping tile x tile pieces blended with Hann windows (float32 windows,
+    as the reference; interpolation.py:117-181,250-290)."""
+    stack = np.asarray(stack, dtype=np.float64)
+    if stack.ndim == 2:
+        stack = stack[None]
+    T, h, w = stack.shape
+    mag = int(mag)
+    out = np.zeros((T, h * mag, w * mag))
+    for t in range(T):
+        f = stack[t]
+        if h <= tile and w <= tile:
+            out[t] = fht_interpolate_frame(f, mag)
+            continue
+        step = max(1, tile - 2 * overlap)
+        acc = np.zeros((h * mag, w * mag))
+        wgt = np.zeros((h * mag, w * mag))
+        for r0 in _tile_starts(h, tile, step):
+            r1 = min(r0 + tile, h)
+            for c0 in _tile_starts(w, tile, step):
+                c1 = min(c0 + tile, w)
+                piece = fht_interpolate_frame(f[r0:r1, c0:c1], mag)
+                wr = np.hanning(piece.shape[0] + 2)[1:-1].astype(np.float32).astype(np.float64)
+                wc = np.hanning(piece.shape[1] + 2)[1:-1].astype(np.float32).astype(np.float64)
+                win = np.outer(wr, wc)
+                acc[r0 * mag:r1 * mag, c0 * mag:c1 * mag] += piece * win
+                wgt[r0 * mag:r1 * mag, c0 * mag:c1 * mag] += win
+        nz = wgt > 0
+        acc[nz] /= wgt[nz]
+        out[t] = acc
+    return out
+
+
+def esrrf_st_fht(stack, magnification=5, radius=1.5, sensitivity=1, doIntensityWeighting=True,
+                 pad_edges=False):
+    """eSRRF_ST with use_fht=True (_le_esrrf.pyx:183-188): FHT-magnified
+    intensity (x m) and Roberts-Cross gradients (x 2m), then RGC with pad_edges."""
+    stack = np.asarray(stack, dtype=np.float64)
+    if stack.ndim == 2:
+        stack = stack[None]
+    m = int(magnification)
+    mag = fht_space_interpolation(stack, m)
+    gc, gr = roberts_cross(stack)
+    return radial_gradient_convergence(fht_space_interpolation(gc, 2 * m),
+                                       fht_space_interpolation(gr, 2 * m), mag, m, radius,
+                                       sensitivity, doIntensityWeighting, pad_edges)
 
 
 # ----------------------------------------------------------------------------

@@ -218,7 +218,8 @@ def load():
     import importlib
 
     t = "nanopyx.core.transform."
-    mods = {m: importlib.import_module(t + m) for m in PYX_MODULES + ["sr_temporal_correlations"]}
+    mods = {m: importlib.import_module(t + m)
+            for m in PYX_MODULES + ["sr_temporal_correlations", "interpolation"]}
     return {
         "CRShiftAndMagnify": mods["_le_interpolation_catmull_rom"].ShiftAndMagnify,
         "GradientRobertsCross": mods["_le_roberts_cross_gradients"].GradientRobertsCross,
@@ -230,6 +231,7 @@ def load():
             mods["sr_temporal_correlations"].calculate_eSRRF_temporal_correlations,
         "calculate_SRRF_temporal_correlations":
             mods["sr_temporal_correlations"].calculate_SRRF_temporal_correlations,
+        "fht_space_interpolation": mods["interpolation"].fht_space_interpolation,
     }
 
 

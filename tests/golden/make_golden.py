@@ -126,6 +126,19 @@ def main():
             g[f"srrf_lag/{T}/{order}"] = np.asarray(
                 R["calculate_SRRF_temporal_correlations"](xl, order, True), dtype=np.float32)
 
+    # FHT interpolation and eSRRF_ST(use_fht=True) (interpolation.py, _le_esrrf.pyx:183-188)
+    xf = blinking_stack(2, 24, 20, 6, seed=18)
+    g["fht/input"] = xf
+    for mag in (2, 5, 10):
+        g[f"fht/{mag}"] = np.asarray(R["fht_space_interpolation"](xf, mag), dtype=np.float32)
+    xt = blinking_stack(1, 260, 40, 20, seed=19)
+    g["fht/tiled_input"] = xt
+    g["fht/tiled_2"] = np.asarray(R["fht_space_interpolation"](xt, 2), dtype=np.float32)
+    for k, (m, pad) in enumerate(((2, False), (3, True), (2, True))):
+        g[f"fht/esrrf_st/{k}"] = np.asarray(R["eSRRF_ST"](verbose=False).run(
+            xf, magnification=m, radius=1.5, sensitivity=1, use_fht=True, pad_edges=pad,
+            run_type="Threaded"), dtype=np.float32)
+
     # macro-pixel correction
     x = (rng.random((2, 20, 25)) + 0.1).astype(np.float32)
     x[0, :, :3] = 0.0

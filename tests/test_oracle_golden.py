@@ -93,6 +93,24 @@ def test_oracle_lag_schedule_reproduces_the_reference_index_errors():
         assert got == fails.get(order, []), order
 
 
+@pytest.mark.parametrize("mag", [2, 5, 10])
+def test_oracle_fht_interpolation(golden, mag):
+    got = O.fht_space_interpolation(golden["fht/input"], mag)
+    assert rel_err(got, golden[f"fht/{mag}"]) <= 1e-5
+
+
+def test_oracle_fht_interpolation_tiled(golden):
+    """Frames over 256 px a side are interpolated in Hann-blended tiles."""
+    got = O.fht_space_interpolation(golden["fht/tiled_input"], 2)
+    assert rel_err(got, golden["fht/tiled_2"]) <= 1e-5
+
+
+@pytest.mark.parametrize("k,m,pad", [(0, 2, False), (1, 3, True), (2, 2, True)])
+def test_oracle_esrrf_st_fht(golden, k, m, pad):
+    got = O.esrrf_st_fht(golden["fht/input"], m, 1.5, 1, True, pad)
+    assert rel_err(got, golden[f"fht/esrrf_st/{k}"]) <= TOL
+
+
 def test_oracle_rejects_bad_correlation():
     with pytest.raises(ValueError):
         O.temporal_correlation(np.zeros((2, 3, 3)), "MAX")
