@@ -40,7 +40,7 @@ CFG = dict(T=500, H=512, W=512, emitters=400, m=5, radius=1.5, sensitivity=2.0,
 SMALL = dict(T=160, fpt=80)
 # DRAM bytes of one fused launch, dram__bytes_read.sum + dram__bytes_write.sum from a
 # 1-pass ncu capture of that launch (large: the full 500-frame launch; small: 160 frames)
-TRAFFIC_BYTES = {"large": 533877248 + 607634688, "small": 169263360 + 207995904}
+TRAFFIC_BYTES = {"large": 531461120 + 604324352, "small": 169977088 + 207399936}
 METRIC = "eSRRF input Mpx*frames/s"
 # frames per reference step: eSRRF_ST and the temporal step scale with the frame
 # count; the per-timepoint macro-pixel correction (2 x ~30 ms on 2560^2) is <1 %
@@ -482,9 +482,15 @@ def bench_uneven_batch(dev, n_stacks=64, seed=3, repeats=2):
         params.append(dict(magnification=int(rng.choice([2, 4, 5])), radius=1.5, sensitivity=1,
                            temporal_correlation=str(rng.choice(["AVG", "VAR", "TAC2"]))))
         mpxf += T * H * H / 1e6
-    b = engine.EsrrfBatch(dev)
-    for x, kw in zip(stacks, params):
-        b.add(x, **kw)
+    def build(tiles):
+        bb = engine.EsrrfBatch(dev, tiles=tiles)
+        for x, kw in zip(stacks, params):
+            bb.add(x, **kw)
+        return bb
+
+    # the tiling autotuner times each kernel key's tilings on this batch
+    tuned = engine.tune_tiling(build)
+    b = build(None)
     b.run(graph=True)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -512,7 +518,9 @@ def bench_uneven_batch(dev, n_stacks=64, seed=3, repeats=2):
                         "pixel values)",
             "mpx_frames": mpxf, "batched_value": mpxf / t_batch, "plain_value": mpxf / t_plain,
             "unit": "Mpx*frames/s", "batched_s": t_batch, "plain_s": t_plain,
-            "speedup": t_plain / t_batch}
+            "speedup": t_plain / t_batch,
+            "tiling": {"autotuned": tuned,
+                       "used": {f"m{m}_J{J}": v for (m, J), v in sorted(b.tiling.items())}}}
 
 
 def bench_sweep(dev, repeats=3):
@@ -529,6 +537,8 @@ def bench_sweep(dev, repeats=3):
 
     x = torch.from_numpy(blinking_stack(200, 256, 256, 150, seed=2)).to(dev)
     sens, radii = [1, 2, 3, 4], [1.0, 1.5, 2.0, 2.5]
+    tuned = engine.tune_tiling(lambda t: engine.SweepGrid(x, 4, sens, radii, tiles=t,
+                                                          plan=False).batch)
     grid = engine.SweepGrid(x, 4, sens, radii)
     grid.run(graph=True)
     torch.cuda.synchronize(dev)
@@ -553,7 +563,10 @@ def bench_sweep(dev, repeats=3):
                         "(16 outputs; one RGC pass per radius shared by 4 sensitivities; "
                         "CUDA-graph replay, planning outside the timed region)",
             "sweep_s": t_sweep, "plain_16_calls_s": t_plain, "speedup": t_plain / t_sweep,
-            "value": mpxf / t_sweep, "unit": "input Mpx*frames/s for the whole grid"}
+            "value": mpxf / t_sweep, "unit": "input Mpx*frames/s for the whole grid",
+            "tiling": {"autotuned": tuned,
+                       "used": {f"m{m}_J{J}": v
+                                for (m, J), v in sorted(grid.batch.tiling.items())}}}
 
 
 SERVED_RATES = (5.0, 10.0, 20.0, 30.0)

@@ -41,7 +41,16 @@ static int invalid(const char* msg) {
 // ---------------------------------------------------------------------------
 // fused-kernel registry
 // ---------------------------------------------------------------------------
-const FusedEntry* fused_entry(int M, int J) {
+const FusedEntry* fused_entry(int M, int J, int variant) {
+  if (variant == 1) {
+    switch (M) {
+      case 2: return fused_entry_m2_alt(J);
+      case 4: return fused_entry_m4_alt(J);
+      case 5: return fused_entry_m5_alt(J);
+      default: return nullptr;
+    }
+  }
+  if (variant != 0) return nullptr;
   switch (M) {
     case 1: return fused_entry_m1(J);
     case 2: return fused_entry_m2(J);
@@ -123,6 +132,7 @@ struct nx_esrrf_plan {
   int JW;           // half-width of the (symmetric) window used by the fused kernel
   nx::RgcScalars sc;
   const nx::FusedEntry* fused;
+  int tile_variant;  // which instantiation `fused` is (0: default tiling)
   int cy_base, cx_base;
   float cy[4], cx[4];
   int device;
@@ -400,6 +410,7 @@ int nx_esrrf_plan_create(nx_esrrf_plan** out, int H, int W, int magnification, f
   p->sc = rgc_scalars(magnification, radius, sensitivity, 0);
   p->JW = std::max(-p->sc.start, p->sc.end - 1);
   p->fused = (p->JW >= 1 && p->JW <= 6) ? fused_entry(magnification, p->JW) : nullptr;
+  p->tile_variant = 0;
   if (p->fused) {
     // instantiations whose shared-memory layout does not fit a CTA use the general path
     const size_t lim = kSmemBudget;
@@ -435,6 +446,33 @@ int nx_esrrf_plan_create(nx_esrrf_plan** out, int H, int W, int magnification, f
   }
   *out = p;
   return NX_OK;
+}
+
+int nx_esrrf_plan_set_tile_variant(nx_esrrf_plan* p, int variant) {
+  if (!p) return invalid("plan is NULL");
+  if (!p->fused) {
+    set_error("this plan runs the general (unfused) path: no tilings to choose from");
+    return NX_ERR_UNSUPPORTED;
+  }
+  if (variant < 0 || variant >= kTileVariants) return invalid("tile variant must be 0 or 1");
+  const FusedEntry* e = fused_entry(p->M, p->JW, variant);
+  if (!e) {
+    set_error("magnification %d, window %d has no tile variant %d", p->M, p->JW, variant);
+    return NX_ERR_UNSUPPORTED;
+  }
+  for (int mode = 0; mode < 3; ++mode)
+    if (e->smem[mode](1) > kSmemBudget) {
+      set_error("tile variant %d does not fit a CTA's shared memory at this window", variant);
+      return NX_ERR_UNSUPPORTED;
+    }
+  p->fused = e;
+  p->tile_variant = variant;
+  return NX_OK;
+}
+
+int nx_esrrf_plan_tile_variant(const nx_esrrf_plan* p) {
+  if (!p) return invalid("plan is NULL");
+  return p->fused ? p->tile_variant : NX_ERR_UNSUPPORTED;
 }
 
 int nx_esrrf_weight_table(int magnification, float radius, float* h_out, size_t cap) {

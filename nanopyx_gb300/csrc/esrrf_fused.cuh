@@ -105,7 +105,7 @@ struct TileRows {
 // normalisation) into a double-buffered slot while the consumers work on the
 // current one.  The consumers' RGC is FMA-pipe bound and the preparation is
 // load/ALU bound, so the two overlap on the SM.
-template <int M>
+template <int M, int V = 0>
 struct EsrrfTile {
   // rows per tile: as many consumer warps as the registers allow without
   // spilling (m = 5: 20 consumer + 4 producer warps at 80 registers measured
@@ -118,7 +118,12 @@ struct EsrrfTile {
   // 512; m = 3: 9.23 / 7.60 / 7.75 ms with 128 / 256 / 384; m = 4 (4 rows):
   // 12.12 / 11.82 ms with 128 / 256 (3 rows: 12.41 / 12.48); m = 5: 16.92 /
   // 18.11 ms with 128 / 256.
-  static constexpr int NP = (M <= 2) ? 384 : (M <= 4 ? 256 : 128);
+  // Tile variant V = 1 (instantiated for m = 2, 4, 5) has one producer warp
+  // group fewer (m = 5: 3 warps), for the tiling autotuner to weigh against
+  // the default on a given batch.
+  static constexpr int NP_DEFAULT = (M <= 2) ? 384 : (M <= 4 ? 256 : 128);
+  static constexpr int NP_ALT = (M <= 2) ? 256 : (M <= 4 ? 128 : 96);
+  static constexpr int NP = V == 0 ? NP_DEFAULT : NP_ALT;
   static constexpr int NT = 32 * TY * M + NP;
   // one CTA per SM: registers for the consumers (m = 8 with 2 CTAs per SM at
   // 80 registers measured 11 % slower than 1 CTA)
@@ -131,7 +136,7 @@ struct EsrrfTile {
 // producers share their index and weight work between the two frames.
 // Results are bit-identical to FP = 1 (the same IEEE operations per frame).
 // Instantiations whose FP = 2 shared-memory layout does not fit a CTA use FP = 1.
-template <int M, int J, int TY, int FP>
+template <int M, int J, int TY, int FP, int NP_ = EsrrfTile<M>::NP>
 struct Geo {
   static constexpr int TX = 32;
   static constexpr int W2 = 2 * J + 1;
@@ -155,7 +160,7 @@ struct Geo {
   static constexpr int OX = TX * M;
   static constexpr int RIW = TX + 4;
   static constexpr int NTC = 32 * TY * M;        // consumer threads
-  static constexpr int NP = EsrrfTile<M>::NP;    // producer threads
+  static constexpr int NP = NP_;                 // producer threads
   static constexpr int NT = NTC + NP;
   // prepared passes in flight between producers and consumers (3 or 4
   // measured no faster: the producers keep up)
@@ -207,15 +212,16 @@ constexpr size_t kMaxSmemPerBlock = 227 * 1024;
 constexpr size_t kSmemBudget = kMaxSmemPerBlock - sizeof(FusedParams) - 64;
 
 // compile-time configuration of one instantiation
-template <int M, int J, int MODE>
+template <int M, int J, int MODE, int V = 0>
 struct FusedCfg {
-  static constexpr int TY = EsrrfTile<M>::TY;
+  static constexpr int TY = EsrrfTile<M, V>::TY;
+  static constexpr int NP = EsrrfTile<M, V>::NP;
   static constexpr int NSC = MODE == kModeSum ? kMaxSens : 1;
   // FP = 4 (two frame pairs per pass sharing the table loads) is supported by
   // the code but not selected: it does not fit shared memory with the VAR/TAC2
   // or AVG state at m = 5, and in stack mode it measured 9 % slower.
-  static constexpr int FP = Geo<M, J, TY, 2>::smem_bytes(MODE, NSC) <= kSmemBudget ? 2 : 1;
-  using G = Geo<M, J, TY, FP>;
+  static constexpr int FP = Geo<M, J, TY, 2, NP>::smem_bytes(MODE, NSC) <= kSmemBudget ? 2 : 1;
+  using G = Geo<M, J, TY, FP, NP>;
 };
 
 __device__ __forceinline__ float f4c(const float4& v, int e) {
@@ -241,9 +247,9 @@ struct UnitGeo {
 // ---------------------------------------------------------------------------
 // producer warpgroup: input tiles -> slot s (unit gradients hg, intensity rows ri)
 // ---------------------------------------------------------------------------
-template <int M, int J, int TY, int FP>
+template <int M, int J, int TY, int FP, int NP>
 struct Producer {
-  using G = Geo<M, J, TY, FP>;
+  using G = Geo<M, J, TY, FP, NP>;
   float* inb;
   float* gsm;  // plane 2 fr: gc, 2 fr + 1: gr
   float* t1;   // plane 2 fr: gx, 2 fr + 1: gy (half-grid columns)
@@ -423,6 +429,14 @@ struct Producer {
   }
 };
 
+// Numerator of the horizontal offset of RGC sample (px, ii) from its output's
+// centre, 2 M dx = M (cpx + ii - J) - (2 px + 1); its sign is the sign of the
+// table's a = dx w / d (zero exactly when dx is).
+template <int M, int J>
+__host__ __device__ constexpr int dx_num(int px, int ii) {
+  return M * ((2 * px + 1) / M + ii - J) - (2 * px + 1);
+}
+
 // RGC of one consumer's M outputs for the FP frames of slot hgf.
 // Contribution of sample (phase, offset): (dp < 0) ? w - |u| : 0 with
 // dp = n.(a, b) and u = n x (a, b) (n the unit gradient).
@@ -502,19 +516,43 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
           if (ii < 0 || ii >= G::W2) continue;
           const int sidx = px * G::W2 + ii;
           const float4 T = tb[sidx];
-          const float2 a = make_float2(T.x, T.x), b = make_float2(T.y, T.y);
-          const float2 nb = make_float2(T.z, T.z);
           const float w = T.w;
+          const int dxn = dx_num<M, J>(px, ii);  // compile-time after unrolling
+          if (dxn != 0) {
+            // dp = a (gx + gy rho) and u = a (gy - gx rho), rho = b / a: the
+            // sign of a is the sign of dx, a constant of (px, ii), so
+            // [dp < 0] is a comparison of t1 = gx + gy rho in a fixed
+            // direction, and w - |u| = w + (-|a|) |t2|, t2 = gy - gx rho:
+            // 4 packed FMA-pipe operations per sample pair instead of 6
+            const float2 rho = make_float2(T.x, T.x), nrho = make_float2(T.y, T.y);
+            const float2 nab = make_float2(T.z, T.z);
 #pragma unroll
-          for (int pp = 0; pp < NPR; ++pp) {
-            const float2 gx = make_float2(g[pp].x, g[pp].y), gy = make_float2(g[pp].z, g[pp].w);
-            const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
-            const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
-            const float2 nu = make_float2(__int_as_float(__float_as_int(u.x) | 0x80000000),
-                                          __int_as_float(__float_as_int(u.y) | 0x80000000));
-            const float2 v = __fadd2_rn(make_float2(w, w), nu);
-            const float2 msk = make_float2(dp.x < 0.f ? 1.f : 0.f, dp.y < 0.f ? 1.f : 0.f);
-            acc2[pp][px] = __ffma2_rn(msk, v, acc2[pp][px]);
+            for (int pp = 0; pp < NPR; ++pp) {
+              const float2 gx = make_float2(g[pp].x, g[pp].y), gy = make_float2(g[pp].z, g[pp].w);
+              const float2 t1 = __ffma2_rn(gy, rho, gx);
+              const float2 t2 = __ffma2_rn(gx, nrho, gy);
+              const float2 at2 = make_float2(fabsf(t2.x), fabsf(t2.y));
+              const float2 v = __ffma2_rn(nab, at2, make_float2(w, w));
+              const float2 msk =
+                  dxn > 0 ? make_float2(t1.x < 0.f ? 1.f : 0.f, t1.y < 0.f ? 1.f : 0.f)
+                          : make_float2(t1.x > 0.f ? 1.f : 0.f, t1.y > 0.f ? 1.f : 0.f);
+              acc2[pp][px] = __ffma2_rn(msk, v, acc2[pp][px]);
+            }
+          } else {
+            // dx = 0: dp = gy b, u = -gx b
+            const float2 a = make_float2(T.x, T.x), b = make_float2(T.y, T.y);
+            const float2 nb = make_float2(T.z, T.z);
+#pragma unroll
+            for (int pp = 0; pp < NPR; ++pp) {
+              const float2 gx = make_float2(g[pp].x, g[pp].y), gy = make_float2(g[pp].z, g[pp].w);
+              const float2 dp = __ffma2_rn(gx, a, __fmul2_rn(gy, b));
+              const float2 u = __ffma2_rn(gy, a, __fmul2_rn(gx, nb));
+              const float2 nu = make_float2(__int_as_float(__float_as_int(u.x) | 0x80000000),
+                                            __int_as_float(__float_as_int(u.y) | 0x80000000));
+              const float2 v = __fadd2_rn(make_float2(w, w), nu);
+              const float2 msk = make_float2(dp.x < 0.f ? 1.f : 0.f, dp.y < 0.f ? 1.f : 0.f);
+              acc2[pp][px] = __ffma2_rn(msk, v, acc2[pp][px]);
+            }
           }
         }
       }
@@ -529,10 +567,10 @@ __device__ __forceinline__ void rgc_core(const float* hgf, const float4* tb4, in
   }
 }
 
-template <int M, int J, int TY, int FP, int MODE>
-__global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::MIN_BLOCKS)
+template <int M, int J, int TY, int FP, int MODE, int NP>
+__global__ void __launch_bounds__(32 * TY * M + NP, EsrrfTile<M>::MIN_BLOCKS)
     esrrf_fused_kernel(const __grid_constant__ TmapPack maps, const UnitTable ut) {
-  using G = Geo<M, J, TY, FP>;
+  using G = Geo<M, J, TY, FP, NP>;
   extern __shared__ __align__(128) float sm[];
   __shared__ FusedParams sp;
   __shared__ int s_unit;
@@ -554,7 +592,7 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
   const int warp = tid >> 5;
   const int ty = warp % TY;  // consumers
   const int py = warp / TY;
-  Producer<M, J, TY, FP> prod{sm + G::O_INB, sm + G::O_G, sm + G::O_T1, sm + G::O_HG,
+  Producer<M, J, TY, FP, NP> prod{sm + G::O_INB, sm + G::O_G, sm + G::O_T1, sm + G::O_HG,
                               sm + G::O_RI, rw, tid - G::NTC};
 
   if (tid == 0) {
@@ -601,14 +639,27 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
       const float4* src = reinterpret_cast<const float4*>(sp.tbl);
       for (int i = tid; i < M * G::W2 * 3 * G::NS4; i += G::NT) tb4[i] = src[i];
     } else {
-      // plan layout [py][jj]{a, b, w}[NS4 * 4] -> one (a, b, -b, w) per sample
+      // plan layout [py][jj]{a, b, w}[NS4 * 4] -> one float4 per sample:
+      //   dx != 0: (rho, -rho, -|a|, w) with rho = b / a (see rgc_core);
+      //   dx == 0: (a, b, -b, w) (a = 0);  outside the window: zeros
       constexpr int N4 = G::NS4 * 4;
       const float* src = sp.tbl;
       for (int i = tid; i < M * G::W2 * N4; i += G::NT) {
         const int blk = i / N4, s = i % N4;
+        const float a = src[(blk * 3 + 0) * N4 + s];
         const float b = src[(blk * 3 + 1) * N4 + s];
-        tb4[blk * G::TBLK + s] = make_float4(src[(blk * 3 + 0) * N4 + s], b, -b,
-                                             src[(blk * 3 + 2) * N4 + s]);
+        const float w = src[(blk * 3 + 2) * N4 + s];
+        const int px = s / G::W2, ii = s % G::W2;
+        float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (s < G::NS && w != 0.f) {
+          if (dx_num<M, J>(px, ii) == 0) {
+            e = make_float4(a, b, -b, w);
+          } else if (a != 0.f) {
+            const float rho = __fdiv_rn(b, a);
+            e = make_float4(rho, -rho, -fabsf(a), w);
+          }
+        }
+        tb4[blk * G::TBLK + s] = e;
       }
     }
     cur_item = item;
@@ -972,17 +1023,17 @@ __global__ void __launch_bounds__(32 * TY * M + EsrrfTile<M>::NP, EsrrfTile<M>::
   }  // unit loop
 }
 
-template <int M, int J, int MODE>
+template <int M, int J, int MODE, int V = 0>
 size_t fused_smem_bytes(int ns_cap) {
-  return FusedCfg<M, J, MODE>::G::smem_bytes(MODE, ns_cap);
+  return FusedCfg<M, J, MODE, V>::G::smem_bytes(MODE, ns_cap);
 }
 
-template <int M, int J, int MODE>
+template <int M, int J, int MODE, int V = 0>
 cudaError_t launch_fused(const UnitTable& ut, const TmapPack& maps, int grid,
                          cudaStream_t stream) {
-  using C = FusedCfg<M, J, MODE>;
+  using C = FusedCfg<M, J, MODE, V>;
   using G = typename C::G;
-  auto kern = esrrf_fused_kernel<M, J, C::TY, C::FP, MODE>;
+  auto kern = esrrf_fused_kernel<M, J, C::TY, C::FP, MODE, C::NP>;
   const size_t smem = G::smem_bytes(MODE, MODE == kModeSum ? ut.ns_cap : 1);
   if (smem > kSmemBudget) return cudaErrorInvalidValue;
   static int attr_done = -1;  // device the attributes were last set for
@@ -1004,11 +1055,11 @@ cudaError_t launch_fused(const UnitTable& ut, const TmapPack& maps, int grid,
 }
 
 // resident CTAs per SM of one instantiation (for persistent grids)
-template <int M, int J, int MODE>
+template <int M, int J, int MODE, int V = 0>
 int fused_occupancy(int ns_cap) {
-  using C = FusedCfg<M, J, MODE>;
+  using C = FusedCfg<M, J, MODE, V>;
   using G = typename C::G;
-  auto kern = esrrf_fused_kernel<M, J, C::TY, C::FP, MODE>;
+  auto kern = esrrf_fused_kernel<M, J, C::TY, C::FP, MODE, C::NP>;
   const size_t smem = G::smem_bytes(MODE, MODE == kModeSum ? ns_cap : 1);
   if (smem > kSmemBudget) return 0;
   // cached per device and sensitivity count (queried once; launches ask per call)
@@ -1035,10 +1086,10 @@ struct FusedGeometry {
   int TY, IX, IY, BW, BH;
 };
 
-template <int M, int J>
+template <int M, int J, int V = 0>
 FusedGeometry fused_geometry() {
-  using G = Geo<M, J, EsrrfTile<M>::TY, 1>;
-  return FusedGeometry{EsrrfTile<M>::TY, G::IX, G::IY, G::BW, G::BH};
+  using G = Geo<M, J, EsrrfTile<M, V>::TY, 1>;
+  return FusedGeometry{EsrrfTile<M, V>::TY, G::IX, G::IY, G::BW, G::BH};
 }
 
 }  // namespace nx

@@ -22,7 +22,9 @@ struct FusedEntry {
   FusedSmemFn smem[3];           // dynamic shared memory bytes
   FusedGeometry geo;
 };
-const FusedEntry* fused_entry(int M, int J);  // nullptr if not instantiated
+// variant 0: the default tiling; 1: one producer warp group fewer (m = 2, 4, 5)
+constexpr int kTileVariants = 2;
+const FusedEntry* fused_entry(int M, int J, int variant = 0);  // nullptr if not instantiated
 const FusedEntry* fused_entry_m1(int J);
 const FusedEntry* fused_entry_m2(int J);
 const FusedEntry* fused_entry_m3(int J);
@@ -30,6 +32,9 @@ const FusedEntry* fused_entry_m4(int J);
 const FusedEntry* fused_entry_m5(int J);
 const FusedEntry* fused_entry_m6(int J);
 const FusedEntry* fused_entry_m8(int J);
+const FusedEntry* fused_entry_m2_alt(int J);
+const FusedEntry* fused_entry_m4_alt(int J);
+const FusedEntry* fused_entry_m5_alt(int J);
 
 // ---------------------------------------------------------------------------
 // standalone op launchers (ops.cu)

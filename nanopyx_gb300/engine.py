@@ -14,9 +14,11 @@ sensitivity in the epilogue, so a 4 x 4 (radius x sensitivity) grid costs four
 RGC passes instead of the sixteen full eSRRF runs of the reference sweep
 (``src/nanopyx/core/analysis/parameter_sweep.py:33-37``).
 
-``tune_frames_per_unit`` is the autotuner: it times the batch at several work
-unit sizes (frames per unit) and caches the fastest per GPU and kernel class
-in ``~/.cache/nanopyx_gb300/autotune.json``.
+Two autotuners cache their choices per GPU and kernel key (magnification,
+window J) in ``~/.cache/nanopyx_gb300/autotune.json``: ``tune_tiling`` times a
+batch under each kernel's tilings (the default, and one producer warp group
+fewer for magnifications 2, 4, 5) and ``tune_frames_per_unit`` times one
+reconstruction at several work-unit sizes.
 """
 from __future__ import annotations
 
@@ -32,7 +34,8 @@ import torch
 from . import _native as N
 from ._device import check_image, get_plan, require_cuda, workspace
 
-__all__ = ["EsrrfBatch", "SweepGrid", "esrrf_batch", "sweep_batch", "tune_frames_per_unit"]
+__all__ = ["EsrrfBatch", "SweepGrid", "esrrf_batch", "sweep_batch", "tune_frames_per_unit",
+           "tune_tiling"]
 
 _CACHE_PATH = os.path.join(os.path.expanduser("~"), ".cache", "nanopyx_gb300", "autotune.json")
 _cache_lock = threading.Lock()
@@ -58,8 +61,11 @@ class EsrrfBatch:
     requested correlation order, or the sensitivity order for a sweep item).
     """
 
-    def __init__(self, device=None):
+    def __init__(self, device=None, tiles=None):
         self.device = device if device is not None else require_cuda()
+        # tile variant per (magnification, window J): explicit choices, else the
+        # autotuner's cached ones, else 0 (the default tiling)
+        self.tiles = dict(tiles or {})
         self._specs = []
         self._handle = None
         self._ws = None
@@ -118,19 +124,36 @@ class EsrrfBatch:
             it.d_out = sp["out"].data_ptr()
         return arr
 
+    def kernel_keys(self):
+        """The (magnification, window J) kernel keys of the batch's items."""
+        return sorted({_kernel_key(*sp["key"]) for sp in self._specs})
+
     def plan(self):
         if not self._specs:
             raise ValueError("empty batch")
         L = N.lib()
         items = self._items()
-        h = C.c_void_p()
-        N.check(L.nx_esrrf_batch_create(C.byref(h), C.cast(items, C.c_void_p), len(self._specs)),
-                "eSRRF batch")
-        self._handle = h
-        self._ws = workspace(L.nx_esrrf_batch_workspace_bytes(h), self.device)
-        N.check(L.nx_esrrf_batch_bind(h, self._ws.data_ptr(), self._ws.numel(),
-                                      torch.cuda.current_stream(self.device).cuda_stream),
-                "eSRRF batch")
+        # the plans are shared with other calls: set each item's tiling only for
+        # the batch's creation and binding, which fix it in the batch's kernel
+        # classes and work lists, then restore the default
+        chosen = {}
+        for sp in self._specs:
+            k = _kernel_key(*sp["key"])
+            v = self.tiles.get(k, _cached_tile(k))
+            chosen[k] = v if L.nx_esrrf_plan_set_tile_variant(sp["plan"].handle, v) == N.NX_OK else 0
+        try:
+            h = C.c_void_p()
+            N.check(L.nx_esrrf_batch_create(C.byref(h), C.cast(items, C.c_void_p),
+                                            len(self._specs)), "eSRRF batch")
+            self._handle = h
+            self._ws = workspace(L.nx_esrrf_batch_workspace_bytes(h), self.device)
+            N.check(L.nx_esrrf_batch_bind(h, self._ws.data_ptr(), self._ws.numel(),
+                                          torch.cuda.current_stream(self.device).cuda_stream),
+                    "eSRRF batch")
+        finally:
+            for sp in self._specs:
+                L.nx_esrrf_plan_set_tile_variant(sp["plan"].handle, 0)
+        self.tiling = chosen
         self.outputs = [sp["out"] for sp in self._specs]
         return self
 
@@ -207,8 +230,9 @@ class SweepGrid:
 
     def __init__(self, stack, magnification: int, sensitivities, radii,
                  frames_per_timepoint: int = 0, doIntensityWeighting: bool = True,
-                 macro_pixel_correction: bool = False, frames_per_unit: int = 0):
-        self.batch = b = EsrrfBatch()
+                 macro_pixel_correction: bool = False, frames_per_unit: int = 0,
+                 tiles=None, plan: bool = True):
+        self.batch = b = EsrrfBatch(tiles=tiles)
         t = stack if isinstance(stack, torch.Tensor) else torch.from_numpy(
             np.ascontiguousarray(check_image(stack)))
         t = check_image(t).to(b.device).contiguous()
@@ -220,7 +244,8 @@ class SweepGrid:
                 self.index[(float(r), tuple(g))] = b.add(
                     t, magnification, r, list(g), frames_per_timepoint, "AVG",
                     doIntensityWeighting, macro_pixel_correction, frames_per_unit)
-        b.plan()
+        if plan:
+            b.plan()
 
     def run(self, graph: bool = False, check: bool = True):
         outs = self.batch.run(graph=graph, check=check)
@@ -248,7 +273,7 @@ def sweep_batch(stack, magnification: int, sensitivities, radii, frames_per_time
 # ---------------------------------------------------------------------------
 # bumped whenever the kernels' tiling or unit structure changes, so that tunings
 # made with an older build are not reused
-TUNE_LAYOUT = "ws2"
+TUNE_LAYOUT = "ws3"
 
 
 def _gpu_key():
@@ -264,17 +289,31 @@ def _load_cache():
         return {}
 
 
+def _kernel_key(m, r):
+    """(magnification, window half-width J = int(2 R)): what selects a kernel."""
+    return int(m), int(np.float32(2.0) * np.float32(r))
+
+
 def _cached_fpu(key) -> int:
-    m, r = key
-    J = int(np.float32(2.0) * np.float32(r))
+    m, J = _kernel_key(*key)
     return int(_load_cache().get(_gpu_key(), {}).get(f"m{m}_J{J}", 0))
+
+
+def _cached_tile(kernel_key) -> int:
+    m, J = kernel_key
+    return int(_load_cache().get(_gpu_key(), {}).get(f"m{m}_J{J}_tile", 0))
 
 
 def _store_fpu(gpu_key: str, magnification: int, J: int, fpu: int) -> bool:
     """Record a tuned frames-per-unit; False (and a warning) if the cache is not writable."""
+    return _store(gpu_key, f"m{int(magnification)}_J{int(J)}", int(fpu))
+
+
+def _store(gpu_key: str, name: str, value: int) -> bool:
+    """Record one tuned value; False (and a warning) if the cache is not writable."""
     with _cache_lock:
         data = _load_cache()
-        data.setdefault(gpu_key, {})[f"m{int(magnification)}_J{int(J)}"] = int(fpu)
+        data.setdefault(gpu_key, {})[name] = int(value)
         try:
             os.makedirs(os.path.dirname(_CACHE_PATH), exist_ok=True)
             tmp = f"{_CACHE_PATH}.{os.getpid()}.tmp"
@@ -313,3 +352,48 @@ def tune_frames_per_unit(stack, magnification: int = 5, radius: float = 1.5,
         J = int(np.float32(2.0) * np.float32(radius))
         _store_fpu(_gpu_key(), magnification, J, best)
     return best, times
+
+
+def _time_batch(b, repeats):
+    b.run(check=False)  # plan, warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(repeats):
+        b.run(check=False)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / repeats
+
+
+def tune_tiling(build, repeats: int = 2, save: bool = True):
+    """Autotuner of the kernels' tiling for one batch.
+
+    ``build(tiles)`` returns an unplanned ``EsrrfBatch`` of the workload with
+    the given {(magnification, J): tile variant} choices.  Every kernel key
+    with a second tiling (magnifications 2, 4, 5: one producer warp group
+    fewer) is timed on the whole batch under both, the others held at their
+    current choice; the faster is kept and, with ``save``, cached per GPU (later
+    batches pick it up).  Returns {"m{m}_J{J}": {"variant": v, "ms": {v: ms}}}.
+    """
+    base = build({})
+    keys = base.kernel_keys()
+    choice = {k: 0 for k in keys}
+    t0 = _time_batch(build(dict(choice)), repeats)
+    report = {}
+    for k in keys:
+        trial = dict(choice)
+        trial[k] = 1
+        probe = build(trial)
+        probe.plan()
+        if probe.tiling.get(k, 0) != 1:  # no second tiling for this key
+            report[f"m{k[0]}_J{k[1]}"] = {"variant": 0, "ms": {0: t0}}
+            continue
+        t1 = _time_batch(probe, repeats)
+        report[f"m{k[0]}_J{k[1]}"] = {"variant": 1 if t1 < t0 else 0, "ms": {0: t0, 1: t1}}
+        if t1 < t0:
+            choice[k], t0 = 1, t1
+    if save:
+        for (m, J), v in choice.items():
+            _store(_gpu_key(), f"m{m}_J{J}_tile", v)
+    return report

@@ -77,3 +77,37 @@ def test_frames_per_unit_does_not_change_the_result_beyond_rounding():
     # chunks), which stays at the level of a few float32 ulps of the deviations
     assert rel_err(outs[0][0], outs[1][0]) <= 1e-5
     assert rel_err(outs[0][1], outs[1][1]) <= 1e-5
+
+
+@pytest.mark.parametrize("m", [2, 4, 5])
+def test_second_tiling_gives_identical_results(m):
+    """The alternative tiling (one producer warp group fewer) only changes who
+    prepares the gradient tiles: with the same frame chunking the results are
+    bit-identical."""
+    x = blinking_stack(12, 40, 72, 12, seed=70 + m)
+    outs = []
+    for v in (0, 1):
+        b = engine.EsrrfBatch(tiles={(m, 3): v})
+        b.add(x, m, 1.5, 2, 0, ("VAR", "TAC2"), frames_per_unit=6)
+        b.add(x, m, 1.5, [1, 2], 0, "AVG", frames_per_unit=6)
+        outs.append([o.clone() for o in b.run()])
+        assert b.tiling[(m, 3)] == v
+    for a, c in zip(*outs):
+        assert torch.equal(a, c)
+
+
+def test_tiling_autotuner_records_a_choice_per_kernel_key():
+    x = blinking_stack(16, 64, 64, 20, seed=77)
+
+    def build(tiles):
+        b = engine.EsrrfBatch(tiles=tiles)
+        b.add(x, 5, 1.5, 1, 0, "AVG")
+        b.add(x, 2, 1.5, 1, 0, "TAC2")
+        b.add(x, 3, 1.5, 1, 0, "VAR")
+        return b
+
+    rep = engine.tune_tiling(build, repeats=1, save=False)
+    assert set(rep) == {"m2_J3", "m3_J3", "m5_J3"}
+    assert rep["m3_J3"]["variant"] == 0 and 1 not in rep["m3_J3"]["ms"]  # one tiling only
+    for k in ("m2_J3", "m5_J3"):
+        assert rep[k]["variant"] in (0, 1) and set(rep[k]["ms"]) == {0, 1}
