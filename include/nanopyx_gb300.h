@@ -54,6 +54,17 @@ int nx_esrrf_plan_create(nx_esrrf_plan** plan, int H, int W, int magnification, 
                          float sensitivity, int do_intensity_weighting);
 int nx_esrrf_plan_destroy(nx_esrrf_plan* plan);
 
+/* Tiling of a plan's fused kernel (no reference counterpart: the reference's
+ * CPU loops have no tiles).  Variant 0 is the default tiling; variant 1
+ * (magnifications 2, 4 and 5) runs one producer warp group fewer per CTA.
+ * Batches group items by kernel instantiation, so items whose plans use
+ * different variants run as different kernel classes.  set returns
+ * NX_ERR_UNSUPPORTED when the variant is not instantiated for the plan's
+ * (magnification, window) or the plan has no fused kernel; get returns the
+ * variant or NX_ERR_UNSUPPORTED.  The results do not depend on the variant. */
+int nx_esrrf_plan_set_tile_variant(nx_esrrf_plan* plan, int variant);
+int nx_esrrf_plan_tile_variant(const nx_esrrf_plan* plan);
+
 /* Host-only (no device call): the RGC distance-weight phase table a plan
  * uploads, w[py][px][j][i] for output sub-pixel phase (py, px) and half-grid
  * window offset (j, i) in [-J, J]; returns J (or a negative status).  Writes
@@ -240,6 +251,22 @@ int nx_srrf_temporal_correlation(const float* d_stack, int T, long long n_pixels
 size_t nx_srrf_acrf_workspace_bytes(int T, long long n_pixels);
 int nx_srrf_acrf_integrated(const float* d_stack, int T, long long n_pixels, int order,
                             float* d_out, void* d_ws, size_t ws_bytes, void* stream);
+
+/* Fourier interpolation (the use_fht=True path of eSRRF_ST): every frame
+ * (T, H, W) -> (T, H*m, W*m), mirror padding to a power-of-two square,
+ * zero-padded spectrum, rescale onto the frame's [min, max], central crop;
+ * frames over 256 px a side in overlapping 256-pixel tiles blended with Hann
+ * windows.  The plan holds the tile layout, the interpolation operators of
+ * every padded size (float64, rounded once) and the blending weights; the
+ * transform runs as batched FP32 GEMMs.
+ *   src/nanopyx/core/transform/interpolation.py:22-290 (fht_space_interpolation)
+ *   src/nanopyx/core/transform/_le_esrrf.pyx:183-188                          */
+typedef struct nx_fht_plan nx_fht_plan;
+int nx_fht_plan_create(nx_fht_plan** plan, int H, int W, int magnification);
+int nx_fht_plan_destroy(nx_fht_plan* plan);
+size_t nx_fht_workspace_bytes(const nx_fht_plan* plan, int T);
+int nx_fht_interpolate(const nx_fht_plan* plan, const float* d_in, int T, float* d_out, void* d_ws,
+                       size_t ws_bytes, void* stream);
 
 /* Macro-pixel correction in place on (S, rowsM, colsM).
  *   src/nanopyx/core/transform/mpcorrector.pyx:7-73                         */

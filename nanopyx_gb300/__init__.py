@@ -10,8 +10,8 @@ from .methods import (SRRF, ESRRFAccumulator, Workflow, eSRRF, esrrf_device, esr
                       run_esrrf_parameter_sweep)
 from .transform import (CRShiftAndMagnify, GradientRobertsCross, RadialGradientConvergence,
                         Radiality, ShiftAndMagnify, calculate_eSRRF_temporal_correlations,
-                        calculate_SRRF_temporal_correlations, eSRRF_ST, macro_pixel_corrector,
-                        value2array)
+                        calculate_SRRF_temporal_correlations, eSRRF_ST, fht_space_interpolation,
+                        macro_pixel_corrector, value2array)
 
 __version__ = "0.1.0"
 
@@ -20,5 +20,6 @@ __all__ = [
     "run_esrrf_parameter_sweep", "ShiftAndMagnify", "CRShiftAndMagnify", "GradientRobertsCross",
     "RadialGradientConvergence", "Radiality", "calculate_eSRRF_temporal_correlations",
     "calculate_SRRF_temporal_correlations", "macro_pixel_corrector", "check_image",
-    "value2array", "LiquidEngine", "NativeLibraryError", "DeviceTimeoutError",
+    "value2array", "fht_space_interpolation", "LiquidEngine", "NativeLibraryError",
+    "DeviceTimeoutError",
 ]

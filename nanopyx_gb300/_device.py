@@ -137,3 +137,41 @@ def get_plan(H: int, W: int, magnification: int, radius: float, sensitivity: flo
         else:
             _plans.move_to_end(key)
         return p
+
+
+class _FhtPlan:
+    __slots__ = ("handle", "key")
+
+    def __init__(self, key):
+        self.key = key
+        h = C.c_void_p()
+        _, H, W, m = key
+        N.check(N.lib().nx_fht_plan_create(C.byref(h), H, W, m), "FHT plan")
+        self.handle = h
+
+    def __del__(self):
+        try:
+            if self.handle:
+                N.lib().nx_fht_plan_destroy(self.handle)
+        except Exception:
+            pass
+
+
+_fht_plans: "collections.OrderedDict" = collections.OrderedDict()
+
+
+def get_fht_plan(H: int, W: int, magnification: int) -> _FhtPlan:
+    """Cached per-device Fourier-interpolation plan (tile layout, float64-derived
+    operators and blending weights on the device)."""
+    require_cuda()
+    key = (torch.cuda.current_device(), int(H), int(W), int(magnification))
+    with _plans_lock:
+        p = _fht_plans.get(key)
+        if p is None:
+            p = _FhtPlan(key)
+            _fht_plans[key] = p
+            while len(_fht_plans) > 16:
+                _fht_plans.popitem(last=False)
+        else:
+            _fht_plans.move_to_end(key)
+        return p

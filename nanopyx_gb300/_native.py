@@ -59,6 +59,8 @@ _SIGS = {
     "nx_last_error": (C.c_char_p, []),
     "nx_esrrf_plan_create": (_I, [C.POINTER(_P), _I, _I, _I, _FL, _FL, _I]),
     "nx_esrrf_plan_destroy": (_I, [_P]),
+    "nx_esrrf_plan_set_tile_variant": (_I, [_P, _I]),
+    "nx_esrrf_plan_tile_variant": (_I, [_P]),
     "nx_esrrf_weight_table": (_I, [_I, _FL, _P, _SZ]),
     "nx_esrrf_st_workspace_bytes": (_SZ, [_P, _I]),
     "nx_esrrf_st": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
@@ -91,6 +93,10 @@ _SIGS = {
     "nx_srrf_temporal_correlation": (_I, [_P, _I, _LL, _I, _P, _P]),
     "nx_srrf_acrf_workspace_bytes": (_SZ, [_I, _LL]),
     "nx_srrf_acrf_integrated": (_I, [_P, _I, _LL, _I, _P, _P, _SZ, _P]),
+    "nx_fht_plan_create": (_I, [C.POINTER(_P), _I, _I, _I]),
+    "nx_fht_plan_destroy": (_I, [_P]),
+    "nx_fht_workspace_bytes": (_SZ, [_P, _I]),
+    "nx_fht_interpolate": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
     "nx_macro_pixel_workspace_bytes": (_SZ, [_I, _I]),
     "nx_macro_pixel_correct": (_I, [_P, _I, _I, _I, _I, _P, _SZ, _P]),
     "nx_macro_pixel_correct_static": (_I, [_P, _I, _I, _I, _I, _P]),

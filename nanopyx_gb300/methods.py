@@ -81,11 +81,13 @@ def eSRRF(image, magnification: int = 5, radius: float = 1.5, sensitivity: float
 
     ``temporal_correlation`` may also be a sequence of names; the result is then
     a tuple with one squeezed array per name, computed in a single pass.
-    ``pad_edges`` has no effect on this (non-FHT) path, as in the reference.
+    ``pad_edges`` only acts with ``use_fht=True``, as in the reference.
     """
-    if use_fht:
-        raise NotImplementedError("use_fht=True (Fourier interpolation) is not implemented")
     names = _corr_list(temporal_correlation)
+    if use_fht:
+        return _esrrf_fht(image, magnification, radius, sensitivity, frames_per_timepoint, names,
+                          isinstance(temporal_correlation, str), doIntensityWeighting,
+                          macro_pixel_correction, pad_edges)
     if isinstance(image, torch.Tensor) and image.is_cuda:
         st = to_device_stack(image)
         out = esrrf_device(st.t, magnification, radius, sensitivity, frames_per_timepoint,
@@ -98,6 +100,33 @@ def eSRRF(image, magnification: int = 5, radius: float = 1.5, sensitivity: float
                           macro_pixel_correction)
         parts = [np.squeeze(res[i]) for i in range(len(names))]
     return parts[0] if isinstance(temporal_correlation, str) else tuple(parts)
+
+
+def _esrrf_fht(image, magnification, radius, sensitivity, frames_per_timepoint, names, single,
+               iw, mpc, pad_edges):
+    """eSRRF() with use_fht=True: per timepoint the Fourier-path eSRRF_ST stack,
+    then the temporal correlation and the macro-pixel correction of each name
+    (eSRRF_workflow.py:76-121), all on the device."""
+    from .transform import _esrrf_st_fht, calculate_eSRRF_temporal_correlations, \
+        macro_pixel_corrector
+
+    on_dev = isinstance(image, torch.Tensor) and image.is_cuda
+    st = to_device_stack(image)
+    x = st.t
+    T = x.shape[0]
+    fpt = T if frames_per_timepoint == 0 or frames_per_timepoint > T else int(frames_per_timepoint)
+    m = int(magnification)
+    res = {n: [] for n in names}
+    for a in range(0, T, fpt):
+        rgc = _esrrf_st_fht(x[a:a + fpt].contiguous(), m, radius, sensitivity, iw, pad_edges)
+        for n in names:
+            tc = calculate_eSRRF_temporal_correlations(rgc, n)
+            res[n].append(macro_pixel_corrector(tc[None], m)[0] if mpc else tc)
+    parts = []
+    for n in names:
+        o = torch.squeeze(torch.stack(res[n]))
+        parts.append(o if on_dev else o.cpu().numpy())
+    return parts[0] if single else tuple(parts)
 
 
 def upload_segments(T: int, fpt: int):

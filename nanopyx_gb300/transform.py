@@ -23,14 +23,14 @@ import numpy as np
 import torch
 
 from . import _native as N
-from ._device import (DeviceStack, check_image, get_plan, require_cuda, stream_ptr,
-                      to_device_stack, workspace)
+from ._device import (DeviceStack, check_image, get_fht_plan, get_plan, require_cuda,
+                      stream_ptr, to_device_stack, workspace)
 from .liquid import LiquidEngine
 
 __all__ = ["ShiftAndMagnify", "CRShiftAndMagnify", "GradientRobertsCross",
            "RadialGradientConvergence", "Radiality", "eSRRF_ST", "value2array",
            "calculate_eSRRF_temporal_correlations", "calculate_SRRF_temporal_correlations",
-           "macro_pixel_corrector", "check_image"]
+           "macro_pixel_corrector", "check_image", "fht_space_interpolation"]
 
 
 def value2array(v, n_frames: int) -> np.ndarray:
@@ -179,8 +179,10 @@ class Radiality(LiquidEngine):
 class eSRRF_ST(LiquidEngine):
     """eSRRF single task: per-frame RGC maps (T, H*m, W*m) from one fused kernel.
 
-    ``pad_edges`` is accepted and, as on the reference's non-FHT path
-    (``_le_esrrf.pyx:194`` does not forward it), has no effect.
+    ``use_fht=True`` follows the reference's Fourier path (``_le_esrrf.pyx:
+    183-188``): FHT-magnified intensity (x m) and gradients (x 2m), then RGC,
+    which honours ``pad_edges``; on the default path ``pad_edges`` has no
+    effect, as in the reference (``_le_esrrf.pyx:194`` does not forward it).
     """
 
     _designation = "eSRRF_ST"
@@ -203,7 +205,9 @@ class eSRRF_ST(LiquidEngine):
     def _run_cuda(self, image, magnification=5, radius=1.5, sensitivity=1, use_fht=False,
                   doIntensityWeighting=True, pad_edges=False):
         if use_fht:
-            raise NotImplementedError("use_fht=True (Fourier interpolation) is not implemented")
+            img = to_device_stack(image)
+            return img.out(_esrrf_st_fht(img.t, int(magnification), radius, sensitivity,
+                                         doIntensityWeighting, pad_edges))
         img = to_device_stack(image)
         T, H, W = img.shape
         m = int(magnification)
@@ -215,6 +219,71 @@ class eSRRF_ST(LiquidEngine):
                               stream_ptr()), "eSRRF_ST")
         N.check(L.nx_workspace_status(_ptr(ws), stream_ptr()), "eSRRF_ST")
         return img.out(out)
+
+
+def _fht_device(t: torch.Tensor, magnification: int) -> torch.Tensor:
+    """(T, H, W) CUDA float32 -> (T, H*m, W*m) Fourier interpolation."""
+    T, H, W = t.shape
+    m = int(magnification)
+    out = torch.empty((T, H * m, W * m), dtype=torch.float32, device=t.device)
+    if T == 0:
+        return out
+    plan = get_fht_plan(H, W, m)
+    L = N.lib()
+    ws = workspace(L.nx_fht_workspace_bytes(plan.handle, T), t.device)
+    N.check(L.nx_fht_interpolate(plan.handle, _ptr(t), T, _ptr(out), _ptr(ws), ws.numel(),
+                                 stream_ptr()), "FHT interpolation")
+    return out
+
+
+def fht_space_interpolation(image, magnification: int = 2, doMirrorPadding: bool = True,
+                            tile_size: int = 0, overlap: int = 16):
+    """Fourier interpolation of a 2-D image or (T, H, W) stack, the reference's
+    ``fht_space_interpolation`` (interpolation.py:250-290): mirror padding,
+    zero-padded spectrum, rescale onto each frame's [min, max]; frames over 256
+    px a side in Hann-blended 256-pixel tiles.  NumPy in -> NumPy out, CUDA
+    tensor in -> CUDA tensor out."""
+    if not doMirrorPadding or int(tile_size) not in (0, 256) or int(overlap) != 16:
+        raise NotImplementedError("the Fourier interpolation supports the default mirror "
+                                  "padding, 256-pixel tiles and 16-pixel overlap")
+    if isinstance(image, torch.Tensor):
+        t = image.to(torch.float32)
+        on_dev = t.is_cuda
+        t = t.to(require_cuda()).contiguous()
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(image, dtype=np.float32))).to(
+            require_cuda())
+        on_dev = False
+    if t.ndim not in (2, 3):
+        raise ValueError("Input must be 2-D or 3-D array")
+    out = _fht_device(t[None] if t.ndim == 2 else t, int(magnification))
+    if t.ndim == 2:
+        out = out[0]
+    return out if on_dev else out.cpu().numpy()
+
+
+def _esrrf_st_fht(x: torch.Tensor, m: int, radius, sensitivity, iw, pad_edges) -> torch.Tensor:
+    """eSRRF_ST on the Fourier path, in frame chunks that keep the 2m-magnified
+    gradients (2 x 4 m^2 H W floats per frame) near 2 GB."""
+    T, H, W = x.shape
+    out = torch.empty((T, H * m, W * m), dtype=torch.float32, device=x.device)
+    per_frame = 4 * (8 * m * m + 4) * H * W
+    chunk = max(1, min(T, (2 << 30) // max(per_frame, 1)))
+    L = N.lib()
+    s = stream_ptr()
+    for a in range(0, T, chunk):
+        xb = x[a:a + chunk].contiguous()
+        n = xb.shape[0]
+        mag = _fht_device(xb, m)
+        gc = torch.empty_like(xb)
+        gr = torch.empty_like(xb)
+        N.check(L.nx_roberts_cross(_ptr(xb), n, H, W, _ptr(gc), _ptr(gr), s), "Roberts-Cross")
+        gci = _fht_device(gc, 2 * m)
+        gri = _fht_device(gr, 2 * m)
+        N.check(L.nx_rgc(_ptr(gci), _ptr(gri), _ptr(mag), n, H * m, W * m, m, float(radius),
+                         float(sensitivity), 1 if iw else 0, 1 if pad_edges else 0,
+                         _ptr(out[a:a + n]), s), "RadialGradientConvergence")
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -36,8 +36,11 @@ def test_correlation_names_validated_before_any_device_work():
 
 
 def test_unimplemented_options_raise():
+    # the Fourier interpolation runs the reference's default tiling and padding only
     with pytest.raises(NotImplementedError):
-        nx.eSRRF(np.zeros((2, 4, 4), np.float32), use_fht=True)
+        nx.fht_space_interpolation(np.zeros((2, 4, 4), np.float32), 2, tile_size=128)
+    with pytest.raises(NotImplementedError):
+        nx.fht_space_interpolation(np.zeros((2, 4, 4), np.float32), 2, doMirrorPadding=False)
     with pytest.raises(NotImplementedError):
         nx.run_esrrf_parameter_sweep(np.zeros((2, 4, 4), np.float32))
 

@@ -114,3 +114,13 @@ def test_argument_checks_run_before_any_device_work(lib):
     assert b"out of bounds" in lib.nx_last_error()
     assert lib.nx_srrf_acrf_integrated(None, 12, 10, 3, None, None, 0, None) == \
         _native.NX_ERR_INVALID_ARG
+    # tile variants need a plan
+    assert lib.nx_esrrf_plan_set_tile_variant(None, 1) == _native.NX_ERR_INVALID_ARG
+    assert lib.nx_esrrf_plan_tile_variant(None) == _native.NX_ERR_INVALID_ARG
+    # Fourier interpolation: plan arguments are checked on the host
+    h = ctypes.c_void_p()
+    assert lib.nx_fht_plan_create(None, 8, 8, 2) == _native.NX_ERR_INVALID_ARG
+    assert lib.nx_fht_plan_create(ctypes.byref(h), 0, 8, 2) == _native.NX_ERR_INVALID_ARG
+    assert lib.nx_fht_plan_create(ctypes.byref(h), 8, 8, 0) == _native.NX_ERR_INVALID_ARG
+    assert lib.nx_fht_interpolate(None, None, 1, None, None, 0, None) == \
+        _native.NX_ERR_INVALID_ARG
