@@ -428,6 +428,8 @@ def run_gpu_arm(args):
         torch.cuda.empty_cache()
         line["sweep"] = bench_sweep(dev)
         torch.cuda.empty_cache()
+        line["sweep_scored"] = bench_scored_sweep(dev)
+        torch.cuda.empty_cache()
         # arrival-rate sweep of the served stream (rates bracket the device's
         # capacity for this request mix); "served" is the highest rate
         blocks = served_blocks([64, 90, 128, 181, 256, 362, 512, 724, 1024])
@@ -567,6 +569,82 @@ def bench_sweep(dev, repeats=3):
             "tiling": {"autotuned": tuned,
                        "used": {f"m{m}_J{J}": v
                                 for (m, J), v in sorted(grid.batch.tiling.items())}}}
+
+
+def bench_scored_sweep(dev, repeats=3):
+    """The scored sweep of the same grid: ParameterSweep.run -- reconstructions
+    over all, odd and even frames, ErrorMap RSP of all 16 pairs (one lockstep
+    Brent search), FRC of all 16 pairs (one batch of FFTs), QnR.
+
+    Beside it, the compiled reference on bounded samples of the same work: its
+    eSRRF_ST on 4 frames and its ErrorMap + FIRECalculator on one pair's
+    1024 x 1024 images (inputs: this engine's reconstructions of that pair);
+    the reference's whole sweep is extrapolated from those two timings
+    (16 x (200 frames x per-frame time + scoring time)), and the pair's RSP and
+    FRC resolution are compared with this engine's."""
+    import torch
+
+    import nanopyx_gb300 as nx
+    from nanopyx_gb300 import scoring
+    from nanopyx_gb300.synthetic import blinking_stack
+
+    x_np = blinking_stack(200, 256, 256, 150, seed=2)
+    x = torch.from_numpy(x_np).to(dev)
+    sens, radii = [1, 2, 3, 4], [1.0, 1.5, 2.0, 2.5]
+    ps = nx.ParameterSweep()
+    ps.run(x, 4, sens, radii)  # warm-up: plans, kernels, tuned tilings
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        q = ps.run(x, 4, sens, radii)
+    torch.cuda.synchronize(dev)
+    t_sweep = (time.perf_counter() - t0) / repeats
+    t0 = time.perf_counter()
+    rec = ps.reconstructions(x, 4, sens, radii)
+    torch.cuda.synchronize(dev)
+    t1 = time.perf_counter()
+    H, W = rec[0].shape[-2:]
+    em = scoring.error_maps(scoring._frame_mean(x), rec[0][:, :, 0].reshape(16, H, W))
+    torch.cuda.synchronize(dev)
+    t2 = time.perf_counter()
+    frc = ps._fire_grid(rec[1], rec[2])
+    t3 = time.perf_counter()
+    out = {"workload": "scored sweep: 200x256x256, m=4, R in {1,1.5,2,2.5} x s in {1,2,3,4}, "
+                       "AVG; reconstructions (all/odd/even frames), RSP, FRC, QnR",
+           "seconds": t_sweep, "reconstructions_s": t1 - t0, "error_maps_s": t2 - t1,
+           "frc_s": t3 - t2, "brent_evaluations": int(sum(em["evaluations"])),
+           "qnr_best": [sens[int(np.argmax(q)) // 4], radii[int(np.argmax(q)) % 4]]}
+    if cpu_reference_available():
+        from oracle import ref_build
+
+        R = ref_build.load()
+        R["eSRRF_ST"](verbose=False).run(x_np[:2], magnification=4, radius=1.5, sensitivity=1,
+                                         run_type="Threaded")
+        t0 = time.perf_counter()
+        R["eSRRF_ST"](verbose=False).run(x_np[:4], magnification=4, radius=1.5, sensitivity=1,
+                                         run_type="Threaded")
+        t_frame = (time.perf_counter() - t0) / 4
+        si, ri = 1, 1  # s = 2, R = 1.5
+        ref_img = np.mean(x_np, axis=0)
+        t0 = time.perf_counter()
+        emr = R["ErrorMap"]()
+        emr.optimise(ref_img, rec[0][si, ri, 0].cpu().numpy())
+        t1 = time.perf_counter()
+        fire_ref = R["FIRECalculator"]().calculate_fire_number(rec[1][si, ri, 0].cpu().numpy(),
+                                                               rec[2][si, ri, 0].cpu().numpy())
+        t2 = time.perf_counter()
+        t_score = t2 - t0
+        est = 16 * (200 * t_frame + t_score)
+        out["reference"] = {
+            "kind": "reference", "cores": os.cpu_count(),
+            "sample": "compiled reference: eSRRF_ST(Threaded) of 4 frames at m=4; ErrorMap + "
+                      "FIRECalculator of one pair (s=2, R=1.5) at 1024x1024",
+            "esrrf_st_s_per_frame": t_frame, "error_map_s": t1 - t0, "frc_s": t2 - t1,
+            "sweep_s_extrapolated": est,
+            "pair_parity": {"rsp_gpu": em["rsp"][si * 4 + ri], "rsp_reference": emr.getRSP(),
+                            "fire_gpu": float(frc[si, ri]), "fire_reference": float(fire_ref)}}
+        out["speedup_vs_reference_extrapolated"] = est / t_sweep
+    return out
 
 
 SERVED_RATES = (5.0, 10.0, 20.0, 30.0)
@@ -811,6 +889,8 @@ def main():
                          "temporal-correlation kernels")
     ap.add_argument("--ops-frames", type=int, default=100,
                     help="frames of the standalone-op measurement")
+    ap.add_argument("--scored-sweep-only", action="store_true",
+                    help="only the scored parameter sweep (RSP / FRC / QnR)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the uneven-batch, sweep and served-stream measurements")
     ap.add_argument("--served-requests", type=int, default=200,
@@ -830,6 +910,12 @@ def main():
         torch.cuda.set_device(0)
         print(json.dumps(bench_standalone_ops(torch.device("cuda", 0), T=args.ops_frames)),
               flush=True)
+        return 0
+    if args.scored_sweep_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_scored_sweep(torch.device("cuda", 0))), flush=True)
         return 0
     if args.srrf_only:
         import torch

@@ -263,10 +263,65 @@ int nx_srrf_acrf_integrated(const float* d_stack, int T, long long n_pixels, int
  *   src/nanopyx/core/transform/_le_esrrf.pyx:183-188                          */
 typedef struct nx_fht_plan nx_fht_plan;
 int nx_fht_plan_create(nx_fht_plan** plan, int H, int W, int magnification);
+/* Variants: NX_FHT_TILED is the plan above (interpolation.py: half spectrum
+ * along x, 256-pixel tiles).  NX_FHT_FULL_SPECTRUM is the older
+ * _interpolation.pyx form that ErrorMap uses (error_map.pyx:16,52-55): the
+ * whole image as one mirrored square, the full complex spectrum on both axes
+ * (fft2, centred block, ifft2, real part), float32 rescale.
+ *   src/nanopyx/core/transform/_interpolation.pyx:106-200                     */
+#define NX_FHT_TILED 0
+#define NX_FHT_FULL_SPECTRUM 1
+int nx_fht_plan_create_ex(nx_fht_plan** plan, int H, int W, int magnification, int variant);
 int nx_fht_plan_destroy(nx_fht_plan* plan);
 size_t nx_fht_workspace_bytes(const nx_fht_plan* plan, int T);
 int nx_fht_interpolate(const nx_fht_plan* plan, const float* d_in, int T, float* d_out, void* d_ws,
                        size_t ws_bytes, void* stream);
+
+/* Parameter-sweep scoring (src/nanopyx/core/analysis/parameter_sweep.py:99-139).
+ *
+ * Gaussian blur with scipy.ndimage.gaussian_filter's definition, as ErrorMap
+ * applies it (src/nanopyx/core/transform/error_map.pyx:72-77,127-146): axis 0
+ * then axis 1, radius int(4 sigma + 0.5), mode 'reflect'; sigma <= 1e-15
+ * leaves the image as it is.  With affine != 0 the input is first mapped to
+ * alpha * x + beta (float32).  d_in and d_out (H, W) must not overlap.        */
+size_t nx_gaussian_blur_workspace_bytes(int H, int W);
+int nx_gaussian_blur(const float* d_in, int H, int W, double sigma, int affine, float alpha,
+                     float beta, float* d_out, void* d_ws, size_t ws_bytes, void* stream);
+/* The same for n images at once, each with its own sigma (host array) and,
+ * when alpha/beta (host arrays) are given, its own affine map: output image i
+ * (of d_out, (n, H, W)) is the blur of input image src_index[i] of d_in
+ * (i itself when src_index is NULL; indices must lie inside d_in).  Up to 32
+ * images per launch; the Brent searches of several error maps share one.   */
+size_t nx_gaussian_blur_batch_workspace_bytes(int H, int W, int n);
+int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
+                           const double* sigma, const float* alpha, const float* beta,
+                           float* d_out, void* d_ws, size_t ws_bytes, void* stream);
+
+/* Float64 moment sums of `batch` images d_x (batch, n) against one image
+ * d_y (n): per image sum x, sum y, sum x^2, sum x y, sum y^2 and
+ * sum (x - y)^2 (the difference rounded to float32 first) into
+ * d_sums (batch, 6), device memory.  Deterministic.                         */
+size_t nx_moment_sums_workspace_bytes(int batch);
+int nx_moment_sums(const float* d_x, const float* d_y, long long n, int batch, double* d_sums,
+                   void* d_ws, size_t ws_bytes, void* stream);
+
+/* Fourier ring correlation sums of `pairs` image pairs
+ * (src/nanopyx/core/analysis/frc.pyx:108-143,150-179,181-198): in pair q the
+ * N x N windows at (r0, c0) of d_img1 + q stride and d_img2 + q stride (row
+ * pitch `pitch` floats) are Tukey(0.25)-tapered and Fourier transformed; for
+ * every ring radius r = 1 .. N/2 - 2 the reference's sample positions on the
+ * centred spectra are bilinearly interpolated and summed in float64:
+ * d_sums[q][r] = (sum a1 a2 + b1 b2, sum a1^2 + b1^2, sum a2^2 + b2^2,
+ * samples), device memory of pairs x (N/2 - 1) x 4 doubles (row 0 zero).
+ * N even, 6 .. 8192; up to 8 pairs per FFT launch.                          */
+typedef struct nx_frc_plan nx_frc_plan;
+int nx_frc_plan_create(nx_frc_plan** plan, int N);
+int nx_frc_plan_destroy(nx_frc_plan* plan);
+int nx_frc_rings(const nx_frc_plan* plan);
+size_t nx_frc_workspace_bytes(const nx_frc_plan* plan, int pairs);
+int nx_frc_ring_sums(const nx_frc_plan* plan, const float* d_img1, const float* d_img2, int pairs,
+                     long long stride, int pitch, int r0, int c0, double* d_sums, void* d_ws,
+                     size_t ws_bytes, void* stream);
 
 /* Macro-pixel correction in place on (S, rowsM, colsM).
  *   src/nanopyx/core/transform/mpcorrector.pyx:7-73                         */

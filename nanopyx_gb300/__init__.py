@@ -6,8 +6,8 @@ Every computation runs in the CUDA library ``_lib/libnanopyx_gb300.so``
 from ._device import check_image
 from ._native import DeviceTimeoutError, NativeLibraryError
 from .liquid import LiquidEngine
-from .methods import (SRRF, ESRRFAccumulator, Workflow, eSRRF, esrrf_device, esrrf_parameter_sweep,
-                      run_esrrf_parameter_sweep)
+from .methods import SRRF, ESRRFAccumulator, Workflow, eSRRF, esrrf_device, esrrf_parameter_sweep
+from .scoring import ErrorMap, FIRECalculator, ParameterSweep, run_esrrf_parameter_sweep
 from .transform import (CRShiftAndMagnify, GradientRobertsCross, RadialGradientConvergence,
                         Radiality, ShiftAndMagnify, calculate_eSRRF_temporal_correlations,
                         calculate_SRRF_temporal_correlations, eSRRF_ST, fht_space_interpolation,
@@ -21,5 +21,5 @@ __all__ = [
     "RadialGradientConvergence", "Radiality", "calculate_eSRRF_temporal_correlations",
     "calculate_SRRF_temporal_correlations", "macro_pixel_corrector", "check_image",
     "value2array", "fht_space_interpolation", "LiquidEngine", "NativeLibraryError",
-    "DeviceTimeoutError",
+    "DeviceTimeoutError", "ErrorMap", "FIRECalculator", "ParameterSweep",
 ]

@@ -145,8 +145,8 @@ class _FhtPlan:
     def __init__(self, key):
         self.key = key
         h = C.c_void_p()
-        _, H, W, m = key
-        N.check(N.lib().nx_fht_plan_create(C.byref(h), H, W, m), "FHT plan")
+        _, H, W, m, variant = key
+        N.check(N.lib().nx_fht_plan_create_ex(C.byref(h), H, W, m, variant), "FHT plan")
         self.handle = h
 
     def __del__(self):
@@ -160,11 +160,16 @@ class _FhtPlan:
 _fht_plans: "collections.OrderedDict" = collections.OrderedDict()
 
 
-def get_fht_plan(H: int, W: int, magnification: int) -> _FhtPlan:
+FHT_TILED, FHT_FULL_SPECTRUM = 0, 1
+
+
+def get_fht_plan(H: int, W: int, magnification: int, variant: int = FHT_TILED) -> _FhtPlan:
     """Cached per-device Fourier-interpolation plan (tile layout, float64-derived
-    operators and blending weights on the device)."""
+    operators and blending weights on the device).  ``variant``: FHT_TILED
+    (interpolation.py, the use_fht path) or FHT_FULL_SPECTRUM
+    (_interpolation.pyx, ErrorMap's reference interpolation)."""
     require_cuda()
-    key = (torch.cuda.current_device(), int(H), int(W), int(magnification))
+    key = (torch.cuda.current_device(), int(H), int(W), int(magnification), int(variant))
     with _plans_lock:
         p = _fht_plans.get(key)
         if p is None:

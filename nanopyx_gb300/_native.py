@@ -94,9 +94,21 @@ _SIGS = {
     "nx_srrf_acrf_workspace_bytes": (_SZ, [_I, _LL]),
     "nx_srrf_acrf_integrated": (_I, [_P, _I, _LL, _I, _P, _P, _SZ, _P]),
     "nx_fht_plan_create": (_I, [C.POINTER(_P), _I, _I, _I]),
+    "nx_fht_plan_create_ex": (_I, [C.POINTER(_P), _I, _I, _I, _I]),
     "nx_fht_plan_destroy": (_I, [_P]),
     "nx_fht_workspace_bytes": (_SZ, [_P, _I]),
     "nx_fht_interpolate": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
+    "nx_gaussian_blur_workspace_bytes": (_SZ, [_I, _I]),
+    "nx_gaussian_blur": (_I, [_P, _I, _I, C.c_double, _I, C.c_float, C.c_float, _P, _P, _SZ, _P]),
+    "nx_gaussian_blur_batch_workspace_bytes": (_SZ, [_I, _I, _I]),
+    "nx_gaussian_blur_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "nx_moment_sums_workspace_bytes": (_SZ, [_I]),
+    "nx_moment_sums": (_I, [_P, _P, C.c_longlong, _I, _P, _P, _SZ, _P]),
+    "nx_frc_plan_create": (_I, [C.POINTER(_P), _I]),
+    "nx_frc_plan_destroy": (_I, [_P]),
+    "nx_frc_rings": (_I, [_P]),
+    "nx_frc_workspace_bytes": (_SZ, [_P, _I]),
+    "nx_frc_ring_sums": (_I, [_P, _P, _P, _I, C.c_longlong, _I, _I, _I, _P, _P, _SZ, _P]),
     "nx_macro_pixel_workspace_bytes": (_SZ, [_I, _I]),
     "nx_macro_pixel_correct": (_I, [_P, _I, _I, _I, _I, _P, _SZ, _P]),
     "nx_macro_pixel_correct_static": (_I, [_P, _I, _I, _I, _I, _P]),

@@ -183,16 +183,24 @@ __global__ void fht_zminmax_kernel(const float* __restrict__ Z, long long n,
 
 // rescale onto the tile's [min, max] (the reference's float32 steps
 // -= out_min, *= scale, += orig_min), crop, and either store (one piece) or
-// add the Hann-weighted piece (tiled: output += piece * outer(wr, wc))
+// add the Hann-weighted piece (tiled: output += piece * outer(wr, wc)).
+// The scale is a float64 quotient of the float32 extremes rounded once
+// (interpolation.py takes the extremes as Python floats), or float32
+// arithmetic throughout (f32_scale: _interpolation.pyx keeps them in C floats).
 __global__ void fht_finish_kernel(const float* __restrict__ Z, int L, const int* __restrict__ mm,
                                   int oh, int ow, int y_roi, int x_roi,
                                   const float* __restrict__ wr, const float* __restrict__ wc,
-                                  float* __restrict__ out, int outH, int outW, int R0, int C0) {
+                                  float* __restrict__ out, int outH, int outW, int R0, int C0,
+                                  int f32_scale) {
   const int z = blockIdx.y;
   const float lo = unordered(mm[4 * z]), hi = unordered(mm[4 * z + 1]);
   const float zlo = unordered(mm[4 * z + 2]), zhi = unordered(mm[4 * z + 3]);
   const bool resc = zhi != zlo;
-  const float scale = resc ? __fdiv_rn(__fsub_rn(hi, lo), __fsub_rn(zhi, zlo)) : 1.f;
+  float scale = 1.f;
+  if (resc)
+    scale = f32_scale ? __fdiv_rn(__fsub_rn(hi, lo), __fsub_rn(zhi, zlo))
+                      : __double2float_rn(__ddiv_rn((double)hi - (double)lo,
+                                                    (double)zhi - (double)zlo));
   const float* zp = Z + (size_t)z * L * L;
   float* o = out + (size_t)z * outH * outW;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)oh * ow;
@@ -250,7 +258,7 @@ struct nx_fht_plan {
     int r0, c0, th, tw, ops, kh, kw, y_roi, x_roi;
     float *wr, *wc;  // Hann windows (tiled path), device
   };
-  int H, W, mag, device;
+  int H, W, mag, device, variant;
   bool tiled;
   std::vector<Ops> ops;
   std::vector<Tile> tiles;
@@ -275,7 +283,9 @@ std::vector<int> tile_starts(int dim) {
 // sin(pi (b-a+1) t) / sin(pi t), and (b - a + 1) at t = 0 -- the only integer
 // phase, since t = (i - n mag) / L lies in (-1, 1).  With |t| >= 1 / L the
 // quotient is well conditioned.
-void build_ops(int N, int mag, std::vector<float>& ct, std::vector<float>& acat) {
+// full: both axes keep the whole complex spectrum f = -N/2 .. N/2-1 (the
+// fft2 / centred-block / ifft2 form of _interpolation.pyx:153-200), i.e. C = A.
+void build_ops(int N, int mag, bool full, std::vector<float>& ct, std::vector<float>& acat) {
   const int L = N * mag;
   const int N2 = (N + 1) / 2;
   const int fa = -(N - N2), fb = N2 - 1;  // y frequencies kept
@@ -293,6 +303,11 @@ void build_ops(int N, int mag, std::vector<float>& ct, std::vector<float>& acat)
       const double pa = pi * (fa + fb) * t;
       acat[(size_t)i * 2 * N + n] = (float)(std::cos(pa) * da / L);
       acat[(size_t)i * 2 * N + N + n] = (float)(-std::sin(pa) * da / L);
+      if (full) {
+        ct[(size_t)n * L + i] = acat[(size_t)i * 2 * N + n];
+        ct[(size_t)N * L + (size_t)n * L + i] = (float)(std::sin(pa) * da / L);
+        continue;
+      }
       // C: 2 sum_{k=0}^{K} e^{2 pi i k t} - 1
       const double dc = zero ? (double)(K + 1) : std::sin(pi * (K + 1) * t) / std::sin(pi * t);
       const double pc = pi * K * t;
@@ -333,7 +348,13 @@ using namespace nx;
 extern "C" {
 
 int nx_fht_plan_create(nx_fht_plan** out, int H, int W, int magnification) {
+  return nx_fht_plan_create_ex(out, H, W, magnification, NX_FHT_TILED);
+}
+
+int nx_fht_plan_create_ex(nx_fht_plan** out, int H, int W, int magnification, int variant) {
   if (!out) return nx::set_error("plan out-pointer is NULL"), NX_ERR_INVALID_ARG;
+  if (variant != NX_FHT_TILED && variant != NX_FHT_FULL_SPECTRUM)
+    return nx::set_error("unknown Fourier interpolation variant %d", variant), NX_ERR_INVALID_ARG;
   *out = nullptr;
   if (H < 1 || W < 1) return nx::set_error("image must have H, W >= 1"), NX_ERR_INVALID_ARG;
   if (magnification < 1 || magnification > 64)
@@ -344,8 +365,9 @@ int nx_fht_plan_create(nx_fht_plan** out, int H, int W, int magnification) {
   p->H = H;
   p->W = W;
   p->mag = magnification;
+  p->variant = variant;
   cudaGetDevice(&p->device);
-  p->tiled = H > kFhtTile || W > kFhtTile;
+  p->tiled = variant == NX_FHT_TILED && (H > kFhtTile || W > kFhtTile);
   std::vector<int> rs{0}, cs{0};
   if (p->tiled) {
     rs = tile_starts(H);
@@ -371,7 +393,7 @@ int nx_fht_plan_create(nx_fht_plan** out, int H, int W, int magnification) {
       if (t.ops < 0) {
         nx_fht_plan::Ops o{N, N * magnification, nullptr, nullptr};
         std::vector<float> ct, acat;
-        build_ops(N, magnification, ct, acat);
+        build_ops(N, magnification, variant == NX_FHT_FULL_SPECTRUM, ct, acat);
         int rc = fht_upload(p, ct, &o.ct);
         if (!rc) rc = fht_upload(p, acat, &o.acat);
         if (rc) {
@@ -485,7 +507,7 @@ int nx_fht_interpolate(const nx_fht_plan* p, const float* d_in, int T, float* d_
       fht_finish_kernel<<<dim3(blocks_for((long long)oh * ow, 256, 1024), (unsigned)tc), 256, 0,
                           s>>>(Z, L, mm, oh, ow, (L - oh) / 2, (L - ow) / 2,
                                p->tiled ? t.wr : nullptr, p->tiled ? t.wc : nullptr, out, outH,
-                               outW, t.r0 * mag, t.c0 * mag);
+                               outW, t.r0 * mag, t.c0 * mag, p->variant == NX_FHT_FULL_SPECTRUM);
       NX_CUDA_TRY(cudaGetLastError());
     }
     if (p->tiled) {

@@ -1,0 +1,683 @@
+// Scoring of the eSRRF parameter sweep on the GPU: the numeric kernels behind
+// ErrorMap (RSP / RSE) and FIRECalculator (FRC) that the reference's
+// ParameterSweep calls per grid point
+// (src/nanopyx/core/analysis/parameter_sweep.py:99-139).
+//
+// * Gaussian blur with scipy.ndimage.gaussian_filter's definition (the
+//   reference's error_map.pyx:72-77,127-146): separable, axis 0 then axis 1,
+//   kernel radius int(4 sigma + 0.5), weights exp(-x^2 / (2 sigma^2))
+//   normalised to sum 1, mode 'reflect' (d c b a | a b c d | d c b a); an axis
+//   with sigma <= 1e-15 is left as it is.  Where the kernel is longer than the
+//   reflection period 2n the taps are folded onto it (the extension is
+//   periodic), so any sigma costs at most 2n taps per output.
+// * Moment sums of image pairs in float64 (regression, Pearson correlation and
+//   RMSE of the error map), deterministic: fixed per-block partials, then one
+//   block in fixed order.
+// * FRC ring sums (frc.pyx:108-143,150-179): crop to the even square, Tukey
+//   taper, 2-D FFT of both images (Stockham autosort, mixed radix, one CTA per
+//   line, twiddles from a float64 table rounded once), and per ring radius the
+//   bilinearly interpolated products a1 a2 + b1 b2, a1^2 + b1^2, a2^2 + b2^2
+//   of the centred spectra summed in float64 over the reference's own sample
+//   positions (float32 angles i * fl(1/r), cos/sin as the reference forms
+//   them).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace nx {
+namespace {
+
+constexpr int kSumBlocks = 256;  // partial-sum blocks of the moment reduction
+constexpr int kSumFields = 6;    // sx, sy, sxx, sxy, syy, s(x-y)^2
+constexpr int kFftThreads = 256;
+constexpr int kMaxFftN = 8192;   // two complex line buffers in shared memory
+constexpr int kFrcChunk = 8;     // image pairs per FFT launch
+
+__host__ __device__ inline long long reflect_index(long long i, long long n) {
+  // 'reflect' extension of [0, n): period 2n, the second half mirrored
+  const long long p = 2 * n;
+  long long m = i % p;
+  if (m < 0) m += p;
+  return m < n ? m : p - 1 - m;
+}
+
+// ---------------------------------------------------------------------------
+// Gaussian blur, a batch of images per launch, each with its own sigma (and
+// affine map): the Brent searches of several error maps advance in lockstep
+// ---------------------------------------------------------------------------
+struct BlurAxis {
+  int taps;    // number of weights
+  int offset;  // sample index of weight 0 relative to the output index
+  int fold;    // weights folded onto the reflection period
+};
+
+constexpr int kBlurBatch = 32;  // images per launch
+struct BlurBatch {
+  int n, affine;
+  int src[kBlurBatch];  // image index in the input stack
+  int radius[kBlurBatch];
+  double sigma[kBlurBatch];
+  float alpha[kBlurBatch], beta[kBlurBatch];
+  BlurAxis ax[2][kBlurBatch];  // taps == 1, offset 0: axis left as it is
+};
+
+// scipy's weights of one image and axis (blockIdx.x, blockIdx.y), in float64,
+// normalised, folded onto the reflection period when the kernel is longer
+__global__ void gauss_weights_kernel(const __grid_constant__ BlurBatch b, int H, int W,
+                                     float* __restrict__ w0, float* __restrict__ w1) {
+  __shared__ double red[256];
+  const int z = blockIdx.x, axis = blockIdx.y;
+  const int n = axis ? W : H;
+  float* w = axis ? w1 + (size_t)z * 2 * W : w0 + (size_t)z * 2 * H;
+  const BlurAxis ax = b.ax[axis][z];
+  const double sigma = b.sigma[z];
+  const int radius = b.radius[z];
+  if (!(sigma > 1e-15)) {
+    if (threadIdx.x == 0) w[0] = 1.f;
+    return;
+  }
+  const double c = -0.5 / (sigma * sigma);
+  double part = 0.0;
+  for (int k = threadIdx.x; k <= 2 * radius; k += blockDim.x) {
+    const double x = (double)(k - radius);
+    part += exp(c * x * x);
+  }
+  red[threadIdx.x] = part;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double total = red[0];
+  if (!ax.fold) {
+    for (int k = threadIdx.x; k <= 2 * radius; k += blockDim.x) {
+      const double x = (double)(k - radius);
+      w[k] = (float)(exp(c * x * x) / total);
+    }
+    return;
+  }
+  // folded: weight j collects every tap offset d with d = j (mod 2n)
+  const int p = 2 * n;
+  for (int j = threadIdx.x; j < p; j += blockDim.x) {
+    double acc = 0.0;
+    const long long d0 = j - (long long)((j + radius) / p) * p;  // smallest d >= -radius
+    for (long long d = d0; d <= radius; d += p) acc += exp(c * (double)d * (double)d) / total;
+    w[j] = (float)acc;
+  }
+}
+
+// axis 0: out[z][y][x] = sum_j w[j] * src[reflect(y + offset + j)][x], the
+// source mapped to alpha * v + beta first when the batch is affine
+__global__ void blur_axis0_kernel(const __grid_constant__ BlurBatch b,
+                                  const float* __restrict__ in, int H, int W,
+                                  const float* __restrict__ w0, float* __restrict__ mid) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= W || y >= H) return;
+  const float* src = in + (size_t)b.src[z] * H * W;
+  const float* w = w0 + (size_t)z * 2 * H;
+  const BlurAxis ax = b.ax[0][z];
+  const float alpha = b.alpha[z], beta = b.beta[z];
+  float acc = 0.f;
+  for (int j = 0; j < ax.taps; ++j) {
+    long long r = (long long)y + ax.offset + j;
+    if (r < 0 || r >= H) r = reflect_index(r, H);
+    float v = __ldg(src + (size_t)r * W + x);
+    if (b.affine) v = __fadd_rn(__fmul_rn(alpha, v), beta);
+    acc = fmaf(__ldg(w + j), v, acc);
+  }
+  mid[((size_t)z * H + y) * W + x] = acc;
+}
+
+// axis 1: the row segment with its reflected halo staged in shared memory
+// when it fits, else read through the cache
+constexpr int kRowTile = 256;
+__global__ void blur_axis1_kernel(const __grid_constant__ BlurBatch b,
+                                  const float* __restrict__ mid, int H, int W,
+                                  const float* __restrict__ w1, int staged,
+                                  float* __restrict__ out) {
+  extern __shared__ float seg[];
+  const int y = blockIdx.y, z = blockIdx.z;
+  const int x0 = blockIdx.x * kRowTile;
+  const float* row = mid + ((size_t)z * H + y) * W;
+  const float* w = w1 + (size_t)z * 2 * W;
+  const BlurAxis ax = b.ax[1][z];
+  if (staged) {
+    const int span = kRowTile + ax.taps - 1;
+    for (int k = threadIdx.x; k < span; k += blockDim.x) {
+      long long c = (long long)x0 + ax.offset + k;
+      if (c < 0 || c >= W) c = reflect_index(c, W);
+      seg[k] = __ldg(row + c);
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < kRowTile; t += blockDim.x) {
+    const int x = x0 + t;
+    if (x >= W) break;
+    float acc = 0.f;
+    if (staged) {
+      for (int j = 0; j < ax.taps; ++j) acc = fmaf(__ldg(w + j), seg[t + j], acc);
+    } else {
+      for (int j = 0; j < ax.taps; ++j) {
+        long long c = (long long)x + ax.offset + j;
+        if (c < 0 || c >= W) c = reflect_index(c, W);
+        acc = fmaf(__ldg(w + j), __ldg(row + c), acc);
+      }
+    }
+    out[((size_t)z * H + y) * W + x] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Moment sums of (x, y) pairs, float64
+// ---------------------------------------------------------------------------
+__device__ inline void block_sum6(double (&v)[kSumFields], double* red /* [6][blockDim] */) {
+  for (int f = 0; f < kSumFields; ++f) red[f * blockDim.x + threadIdx.x] = v[f];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int f = 0; f < kSumFields; ++f)
+        red[f * blockDim.x + threadIdx.x] += red[f * blockDim.x + threadIdx.x + s];
+    __syncthreads();
+  }
+  for (int f = 0; f < kSumFields; ++f) v[f] = red[f * blockDim.x];
+}
+
+__global__ void __launch_bounds__(256) moment_partial_kernel(const float* __restrict__ x,
+                                                             const float* __restrict__ y,
+                                                             long long n,
+                                                             double* __restrict__ part) {
+  __shared__ double red[kSumFields * 256];
+  const int z = blockIdx.y;
+  const float* xs = x + (size_t)z * n;
+  const float* ys = y;  // the second image is shared by the batch
+  double v[kSumFields] = {0, 0, 0, 0, 0, 0};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double a = xs[i], b = ys[i];
+    const double d = (double)__fsub_rn(xs[i], ys[i]);
+    v[0] += a;
+    v[1] += b;
+    v[2] += a * a;
+    v[3] += a * b;
+    v[4] += b * b;
+    v[5] += d * d;
+  }
+  block_sum6(v, red);
+  if (threadIdx.x == 0)
+    for (int f = 0; f < kSumFields; ++f)
+      part[((size_t)z * gridDim.x + blockIdx.x) * kSumFields + f] = v[f];
+}
+
+__global__ void __launch_bounds__(256) moment_final_kernel(const double* __restrict__ part,
+                                                           int nparts, double* __restrict__ out) {
+  __shared__ double red[kSumFields * 256];
+  const int z = blockIdx.x;
+  double v[kSumFields] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+    for (int f = 0; f < kSumFields; ++f) v[f] += part[((size_t)z * nparts + b) * kSumFields + f];
+  block_sum6(v, red);
+  if (threadIdx.x == 0)
+    for (int f = 0; f < kSumFields; ++f) out[(size_t)z * kSumFields + f] = v[f];
+}
+
+// ---------------------------------------------------------------------------
+// FFT: one line of N complex values per CTA, Stockham autosort in shared
+// memory.  Stage s with radix R after Ns = product of the earlier radices:
+// group j < N/R, k = j mod Ns, inputs x[j + r N/R], outputs
+// y[(j / Ns) Ns R + k + q Ns] = sum_r x[j + r N/R] w^(r (k + q Ns) N / (Ns R)),
+// w = e^{-2 pi i / N} (one table lookup per term, exponent reduced mod N).
+// ---------------------------------------------------------------------------
+struct FftPlanDev {
+  int N, nstages;
+  int radix[24];
+};
+
+__device__ inline float2 cmul(float2 a, float2 b) {
+  return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                     __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ inline float2 cadd(float2 a, float2 b) {
+  return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+__device__ inline float2 csub(float2 a, float2 b) {
+  return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+
+// Lines of image z = 2 pair + which (blockIdx.y).
+// mode 0: real input lines: row y of image `which` of the pair, at
+//         (r0 + y, c0 ..) of a plane with row pitch `pitch` (planes
+//         `stride` floats apart), multiplied by taper_x then taper_y as the
+//         reference does
+// mode 1: complex input lines (contiguous N x N per image)
+// output: the transformed line written as column `line` of dst (transpose)
+__global__ void __launch_bounds__(kFftThreads) fft_lines_kernel(
+    const __grid_constant__ FftPlanDev plan, const float2* __restrict__ tw, int mode,
+    const float* __restrict__ rsrc0, const float* __restrict__ rsrc1, long long stride, int pitch,
+    int r0, int c0, const float* __restrict__ taper, const float2* __restrict__ csrc,
+    float2* __restrict__ dst) {
+  extern __shared__ float2 buf[];
+  const int N = plan.N;
+  const int line = blockIdx.x, z = blockIdx.y;
+  float2* a = buf;
+  float2* b = buf + N;
+  if (mode == 0) {
+    const float* row = ((z & 1) ? rsrc1 : rsrc0) + (size_t)(z >> 1) * stride +
+                       (size_t)(r0 + line) * pitch + c0;
+    const float ty = taper[line];
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+      a[i] = make_float2(__fmul_rn(__fmul_rn(row[i], taper[i]), ty), 0.f);
+  } else {
+    const float2* row = csrc + ((size_t)z * N + line) * N;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) a[i] = row[i];
+  }
+  __syncthreads();
+  int Ns = 1;
+  for (int s = 0; s < plan.nstages; ++s) {
+    const int R = plan.radix[s];
+    const int G = N / R;          // groups
+    const int step = N / (Ns * R);
+    for (int j = threadIdx.x; j < G; j += blockDim.x) {
+      const int k = j % Ns;
+      const int base = (j / Ns) * Ns * R + k;
+      if (R == 2) {
+        const float2 t = tw[k * step];
+        const float2 u = a[j], v = cmul(a[j + G], t);
+        b[base] = cadd(u, v);
+        b[base + Ns] = csub(u, v);
+      } else if (R == 4) {
+        const float2 x0 = a[j];
+        const float2 x1 = cmul(a[j + G], tw[k * step]);
+        const float2 x2 = cmul(a[j + 2 * G], tw[2 * k * step]);
+        const float2 x3 = cmul(a[j + 3 * G], tw[3 * k * step]);
+        const float2 s02 = cadd(x0, x2), d02 = csub(x0, x2);
+        const float2 s13 = cadd(x1, x3), d13 = csub(x1, x3);
+        // forward transform: multiply d13 by -i
+        const float2 md = make_float2(d13.y, -d13.x);
+        b[base] = cadd(s02, s13);
+        b[base + Ns] = cadd(d02, md);
+        b[base + 2 * Ns] = csub(s02, s13);
+        b[base + 3 * Ns] = csub(d02, md);
+      } else {
+        for (int q = 0; q < R; ++q) {
+          const long long e0 = (long long)(k + q * Ns) * step;  // < N
+          float2 acc = a[j];
+          for (int r = 1; r < R; ++r) {
+            const float2 t = tw[(int)((e0 * r) % N)];
+            const float2 x = a[j + r * G];
+            acc.x = fmaf(x.x, t.x, fmaf(-x.y, t.y, acc.x));
+            acc.y = fmaf(x.x, t.y, fmaf(x.y, t.x, acc.y));
+          }
+          b[base + q * Ns] = acc;
+        }
+      }
+    }
+    __syncthreads();
+    float2* t = a;
+    a = b;
+    b = t;
+    Ns *= R;
+  }
+  float2* out = dst + (size_t)z * N * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) out[(size_t)i * N + line] = a[i];
+}
+
+// ring sums of the centred product images of pair blockIdx.y; one CTA per
+// ring radius
+__global__ void __launch_bounds__(256) frc_ring_kernel(const float2* __restrict__ F,
+                                                       int N, const float2* __restrict__ pos,
+                                                       const int* __restrict__ ring_start,
+                                                       double* __restrict__ sums_all) {
+  __shared__ double red[kSumFields * 256];
+  const int r = blockIdx.x + 1;
+  const float2* F1 = F + (size_t)blockIdx.y * 2 * N * N;
+  const float2* F2 = F1 + (size_t)N * N;
+  double* sums = sums_all + (size_t)blockIdx.y * (gridDim.x + 1) * 4;
+  const int h = N / 2;
+  double v[kSumFields] = {0, 0, 0, 0, 0, 0};
+  const int s0 = ring_start[r - 1], s1 = ring_start[r];
+  for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+    const float2 p = pos[s];
+    const int xb = (int)p.x, yb = (int)p.y;
+    float fx = __fsub_rn(p.x, (float)xb), fy = __fsub_rn(p.y, (float)yb);
+    if (fx < 0.f) fx = 0.f;
+    if (fy < 0.f) fy = 0.f;
+    float c[4][3];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int yy = yb + (q >> 1), xx = xb + (q & 1);
+      // fftshift: centred index i <-> spectrum index (i + N/2) mod N
+      const size_t idx = (size_t)((yy + h) % N) * N + (xx + h) % N;
+      const float2 u = F1[idx], w = F2[idx];
+      c[q][0] = __fadd_rn(__fmul_rn(u.x, w.x), __fmul_rn(u.y, w.y));
+      c[q][1] = __fadd_rn(__fmul_rn(u.x, u.x), __fmul_rn(u.y, u.y));
+      c[q][2] = __fadd_rn(__fmul_rn(w.x, w.x), __fmul_rn(w.y, w.y));
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      // corners: 0 lower-left, 1 lower-right, 2 upper-left, 3 upper-right
+      const float up = __fadd_rn(c[2][f], __fmul_rn(fx, __fsub_rn(c[3][f], c[2][f])));
+      const float lo = __fadd_rn(c[0][f], __fmul_rn(fx, __fsub_rn(c[1][f], c[0][f])));
+      v[f] += (double)__fadd_rn(lo, __fmul_rn(fy, __fsub_rn(up, lo)));
+    }
+  }
+  block_sum6(v, red);
+  if (threadIdx.x == 0) {
+    sums[(size_t)r * 4 + 0] = v[0];
+    sums[(size_t)r * 4 + 1] = v[1];
+    sums[(size_t)r * 4 + 2] = v[2];
+    sums[(size_t)r * 4 + 3] = (double)(s1 - s0);
+  }
+}
+
+
+BlurAxis blur_axis(double sigma, int radius, int n) {
+  if (!(sigma > 1e-15)) return BlurAxis{1, 0, 0};  // scipy leaves the axis alone
+  if (2LL * radius + 1 > 2LL * n) return BlurAxis{2 * n, 0, 1};
+  return BlurAxis{2 * radius + 1, -radius, 0};
+}
+
+}  // namespace
+}  // namespace nx
+
+// ---------------------------------------------------------------------------
+// FRC plan: FFT factorisation and twiddles, Tukey taper, ring sample positions
+// ---------------------------------------------------------------------------
+struct nx_frc_plan {
+  int N, device;
+  nx::FftPlanDev fft;
+  float2* tw = nullptr;
+  float* taper = nullptr;
+  float2* pos = nullptr;
+  int* ring_start = nullptr;
+  int n_rings = 0;  // rings 1 .. n_rings (the reference's r = 1 .. N/2 - 2)
+};
+
+namespace nx {
+namespace {
+
+void frc_plan_free(nx_frc_plan* p) {
+  cudaFree(p->tw);
+  cudaFree(p->taper);
+  cudaFree(p->pos);
+  cudaFree(p->ring_start);
+  delete p;
+}
+
+// scipy.signal.windows.tukey(M, 0.25), symmetric, float64 then float32
+std::vector<float> tukey_window(int M, double alpha) {
+  std::vector<float> w(M, 1.f);
+  if (M <= 1) return w;
+  const double pi = 3.14159265358979323846;
+  const int width = (int)std::floor(alpha * (M - 1) / 2.0);
+  for (int n = 0; n < M; ++n) {
+    double v = 1.0;
+    if (n <= width)
+      v = 0.5 * (1 + std::cos(pi * (-1 + 2.0 * n / alpha / (M - 1))));
+    else if (n >= M - width - 1)
+      v = 0.5 * (1 + std::cos(pi * (-2.0 / alpha + 1 + 2.0 * n / alpha / (M - 1))));
+    w[n] = (float)v;
+  }
+  return w;
+}
+
+// radices: 4s first, then 2, 3, 5, 7, then remaining prime factors
+bool fft_factor(int N, FftPlanDev& f) {
+  f.N = N;
+  f.nstages = 0;
+  int n = N;
+  auto push = [&](int r) {
+    if (f.nstages >= 24) return false;
+    f.radix[f.nstages++] = r;
+    n /= r;
+    return true;
+  };
+  while (n % 4 == 0)
+    if (!push(4)) return false;
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0)
+      if (!push(p)) return false;
+  for (int p = 11; (long long)p * p <= n; p += 2)
+    while (n % p == 0)
+      if (!push(p)) return false;
+  if (n > 1 && !push(n)) return false;
+  return true;
+}
+
+template <class T>
+int upload(const std::vector<T>& h, T** d) {
+  cudaError_t e = cudaMalloc(d, std::max<size_t>(1, h.size()) * sizeof(T));
+  if (e == cudaSuccess && !h.empty())
+    e = cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? NX_OK : cuda_status(e, "FRC plan upload");
+}
+
+}  // namespace
+}  // namespace nx
+
+using namespace nx;
+
+extern "C" {
+
+size_t nx_gaussian_blur_batch_workspace_bytes(int H, int W, int n) {
+  if (H < 1 || W < 1 || n < 1) return 256;
+  const size_t k = (size_t)std::min(n, kBlurBatch);
+  return 256 + ((k * (2 * (size_t)H + 2 * (size_t)W) * sizeof(float) + 255) / 256) * 256 +
+         k * H * W * sizeof(float);
+}
+
+int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
+                           const double* sigma, const float* alpha, const float* beta,
+                           float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+  if (H < 1 || W < 1 || n < 0) return nx::set_error("need H, W >= 1, n >= 0"), NX_ERR_INVALID_ARG;
+  if (n == 0) return NX_OK;
+  if (!d_in || !d_out || !sigma) return nx::set_error("NULL pointer"), NX_ERR_INVALID_ARG;
+  if ((alpha == nullptr) != (beta == nullptr))
+    return nx::set_error("alpha and beta go together"), NX_ERR_INVALID_ARG;
+  if (!d_ws || ws_bytes < nx_gaussian_blur_batch_workspace_bytes(H, W, n)) {
+    nx::set_error("workspace too small: need %zu bytes",
+                  nx_gaussian_blur_batch_workspace_bytes(H, W, n));
+    return NX_ERR_WORKSPACE;
+  }
+  for (int i = 0; i < n; ++i) {
+    if (!(sigma[i] <= 1e7)) return nx::set_error("sigma must be <= 1e7"), NX_ERR_INVALID_ARG;
+    if (src_index && src_index[i] < 0) return nx::set_error("negative image index"), NX_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t plane = (size_t)H * W;
+  char* base = (char*)d_ws + 256;
+  const size_t k = (size_t)std::min(n, kBlurBatch);  // images per launch
+  float* w0 = (float*)base;                            // k x 2H weights, axis 0
+  float* w1 = w0 + k * 2 * H;                          // k x 2W weights, axis 1
+  float* mid = (float*)(base + ((k * (2 * (size_t)H + 2 * (size_t)W) * sizeof(float) + 255) /
+                                256) * 256);
+  for (int c0 = 0; c0 < n; c0 += kBlurBatch) {
+    BlurBatch b{};
+    b.n = std::min(kBlurBatch, n - c0);
+    b.affine = alpha != nullptr;
+    int max_taps1 = 1;
+    for (int i = 0; i < b.n; ++i) {
+      const int g = c0 + i;
+      b.src[i] = src_index ? src_index[g] : g;
+      b.sigma[i] = sigma[g];
+      b.radius[i] = sigma[g] > 1e-15 ? (int)(4.0 * sigma[g] + 0.5) : 0;
+      b.alpha[i] = alpha ? alpha[g] : 1.f;
+      b.beta[i] = beta ? beta[g] : 0.f;
+      b.ax[0][i] = blur_axis(sigma[g], b.radius[i], H);
+      b.ax[1][i] = blur_axis(sigma[g], b.radius[i], W);
+      max_taps1 = std::max(max_taps1, b.ax[1][i].taps);
+    }
+    gauss_weights_kernel<<<dim3(b.n, 2), 256, 0, s>>>(b, H, W, w0, w1);
+    NX_CUDA_TRY(cudaGetLastError());
+    blur_axis0_kernel<<<dim3((W + 31) / 32, (H + 7) / 8, b.n), dim3(32, 8), 0, s>>>(
+        b, d_in, H, W, w0, mid);
+    NX_CUDA_TRY(cudaGetLastError());
+    const size_t seg = ((size_t)kRowTile + max_taps1 - 1) * sizeof(float);
+    const int staged = seg <= 48 * 1024;
+    blur_axis1_kernel<<<dim3((W + kRowTile - 1) / kRowTile, H, b.n), 256, staged ? seg : 0, s>>>(
+        b, mid, H, W, w1, staged, d_out + (size_t)c0 * plane);
+    NX_CUDA_TRY(cudaGetLastError());
+  }
+  return NX_OK;
+}
+
+size_t nx_gaussian_blur_workspace_bytes(int H, int W) {
+  return nx_gaussian_blur_batch_workspace_bytes(H, W, 1);
+}
+
+int nx_gaussian_blur(const float* d_in, int H, int W, double sigma, int affine, float alpha,
+                     float beta, float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+  if (d_in && d_in == d_out) return nx::set_error("blur cannot run in place"), NX_ERR_INVALID_ARG;
+  return nx_gaussian_blur_batch(d_in, H, W, 1, nullptr, &sigma, affine ? &alpha : nullptr,
+                                affine ? &beta : nullptr, d_out, d_ws, ws_bytes, stream);
+}
+
+size_t nx_moment_sums_workspace_bytes(int batch) {
+  return 256 + (size_t)std::max(batch, 1) * kSumBlocks * kSumFields * sizeof(double);
+}
+
+int nx_moment_sums(const float* d_x, const float* d_y, long long n, int batch, double* d_sums,
+                   void* d_ws, size_t ws_bytes, void* stream) {
+  if (n < 1 || batch < 1) return nx::set_error("need n >= 1, batch >= 1"), NX_ERR_INVALID_ARG;
+  if (!d_x || !d_y || !d_sums) return nx::set_error("NULL pointer"), NX_ERR_INVALID_ARG;
+  if (batch > 65535) return nx::set_error("batch must be <= 65535"), NX_ERR_INVALID_ARG;
+  if (!d_ws || ws_bytes < nx_moment_sums_workspace_bytes(batch)) {
+    nx::set_error("workspace too small: need %zu bytes", nx_moment_sums_workspace_bytes(batch));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* part = (double*)((char*)d_ws + 256);
+  moment_partial_kernel<<<dim3(kSumBlocks, batch), 256, 0, s>>>(d_x, d_y, n, part);
+  NX_CUDA_TRY(cudaGetLastError());
+  moment_final_kernel<<<batch, 256, 0, s>>>(part, kSumBlocks, d_sums);
+  NX_CUDA_TRY(cudaGetLastError());
+  return NX_OK;
+}
+
+int nx_frc_plan_create(nx_frc_plan** out, int N) {
+  if (!out) return nx::set_error("plan out-pointer is NULL"), NX_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (N < 6 || N % 2 || N > kMaxFftN)
+    return nx::set_error("FRC size must be even and in [6, %d]", kMaxFftN), NX_ERR_INVALID_ARG;
+  auto* p = new nx_frc_plan();
+  p->N = N;
+  cudaGetDevice(&p->device);
+  if (!fft_factor(N, p->fft)) {
+    delete p;
+    return nx::set_error("FFT size %d has too many factors", N), NX_ERR_INVALID_ARG;
+  }
+  const double pi = 3.14159265358979323846;
+  std::vector<float2> tw(N);
+  for (int k = 0; k < N; ++k) {
+    const double a = -2.0 * pi * (double)k / N;
+    tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  // ring sample positions, r = 1 .. max_r - 1 with max_r = N/2 - 1
+  // (frc.pyx:150-179): angles fl32(i * fl32(1/r)) below fl32(2 pi), then
+  // x = max_r + 1 + r cos, y = max_r + 1 + r sin, sin = +-sqrt(1 - cos^2)
+  const int max_r = N / 2 - 1;
+  p->n_rings = max_r - 1;
+  std::vector<float2> pos;
+  std::vector<int> start{0};
+  const float limit = (float)(pi * 2);
+  for (int r = 1; r < max_r; ++r) {
+    const float step = (float)(1.0 / r);
+    const long long cnt = (long long)std::ceil((double)limit / (double)step);
+    for (long long i = 0; i < cnt; ++i) {
+      const float ang = (float)i * step;
+      const float ca = (float)std::cos((double)ang);
+      const float c2 = ca * ca;
+      const float om = 1.0f - c2;
+      double sn = std::sqrt((double)om);
+      if ((double)ang > pi) sn = -sn;  // the reference compares with the double pi
+      const float sa = (float)sn;
+      const float rf = (float)r;
+      const float x = (float)(max_r + 1) + rf * ca;
+      const float y = (float)(max_r + 1) + rf * sa;
+      pos.push_back(make_float2(x, y));
+    }
+    start.push_back((int)pos.size());
+  }
+  int rc = upload(tw, &p->tw);
+  if (!rc) rc = upload(tukey_window(N, 0.25), &p->taper);
+  if (!rc) rc = upload(pos, &p->pos);
+  if (!rc) rc = upload(start, &p->ring_start);
+  if (rc) {
+    frc_plan_free(p);
+    return rc;
+  }
+  const int smem = 2 * N * (int)sizeof(float2);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(fft_lines_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) {
+      frc_plan_free(p);
+      return cuda_status(e, "FFT shared memory");
+    }
+  }
+  *out = p;
+  return NX_OK;
+}
+
+int nx_frc_plan_destroy(nx_frc_plan* p) {
+  if (p) frc_plan_free(p);
+  return NX_OK;
+}
+
+int nx_frc_rings(const nx_frc_plan* p) { return p ? p->n_rings : 0; }
+
+size_t nx_frc_workspace_bytes(const nx_frc_plan* p, int pairs) {
+  if (!p || pairs < 1) return 256;
+  return 256 + (size_t)4 * std::min(pairs, kFrcChunk) * p->N * p->N * sizeof(float2);
+}
+
+int nx_frc_ring_sums(const nx_frc_plan* p, const float* d_img1, const float* d_img2, int pairs,
+                     long long stride, int pitch, int r0, int c0, double* d_sums, void* d_ws,
+                     size_t ws_bytes, void* stream) {
+  if (!p) return nx::set_error("plan is NULL"), NX_ERR_INVALID_ARG;
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != p->device) return nx::set_error("plan made on another device"), NX_ERR_INVALID_ARG;
+  if (pairs < 0) return nx::set_error("pairs must be >= 0"), NX_ERR_INVALID_ARG;
+  if (pairs == 0) return NX_OK;
+  if (!d_img1 || !d_img2 || !d_sums) return nx::set_error("NULL pointer"), NX_ERR_INVALID_ARG;
+  if (pitch < p->N || r0 < 0 || c0 < 0 || c0 + p->N > pitch)
+    return nx::set_error("crop window outside the image rows"), NX_ERR_INVALID_ARG;
+  if (pairs > 1 && stride < (long long)(r0 + p->N) * pitch)
+    return nx::set_error("image stride smaller than the crop window"), NX_ERR_INVALID_ARG;
+  if (!d_ws || ws_bytes < nx_frc_workspace_bytes(p, pairs)) {
+    nx::set_error("workspace too small: need %zu bytes", nx_frc_workspace_bytes(p, pairs));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int N = p->N;
+  const int chunk = std::min(pairs, kFrcChunk);
+  float2* T = (float2*)((char*)d_ws + 256);  // (2 chunk, N, N): transposed after pass 1
+  float2* F = T + (size_t)2 * chunk * N * N;  // (2 chunk, N, N): spectra, natural layout
+  const int smem = 2 * N * (int)sizeof(float2);
+  const size_t rows = (size_t)p->n_rings + 1;
+  for (int q0 = 0; q0 < pairs; q0 += chunk) {
+    const int q = std::min(chunk, pairs - q0);
+    fft_lines_kernel<<<dim3(N, 2 * q), kFftThreads, smem, s>>>(
+        p->fft, p->tw, 0, d_img1 + (size_t)q0 * stride, d_img2 + (size_t)q0 * stride, stride,
+        pitch, r0, c0, p->taper, nullptr, T);
+    NX_CUDA_TRY(cudaGetLastError());
+    fft_lines_kernel<<<dim3(N, 2 * q), kFftThreads, smem, s>>>(
+        p->fft, p->tw, 1, nullptr, nullptr, 0, 0, 0, 0, p->taper, T, F);
+    NX_CUDA_TRY(cudaGetLastError());
+    double* out = d_sums + (size_t)q0 * rows * 4;
+    NX_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)q * rows * 4 * sizeof(double), s));
+    frc_ring_kernel<<<dim3(p->n_rings, q), 256, 0, s>>>(F, N, p->pos, p->ring_start, out);
+    NX_CUDA_TRY(cudaGetLastError());
+  }
+  return NX_OK;
+}
+
+}  // extern "C"

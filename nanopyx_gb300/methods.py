@@ -24,7 +24,7 @@ from ._device import check_image, get_plan, stream_ptr, to_device_stack, workspa
 from .transform import (GradientRobertsCross, Radiality, ShiftAndMagnify,  # noqa: F401
                         macro_pixel_corrector)
 
-__all__ = ["eSRRF", "SRRF", "Workflow", "ESRRFAccumulator", "esrrf_parameter_sweep", "run_esrrf_parameter_sweep",
+__all__ = ["eSRRF", "SRRF", "Workflow", "ESRRFAccumulator", "esrrf_parameter_sweep",
            "esrrf_device"]
 
 
@@ -335,12 +335,6 @@ def esrrf_parameter_sweep(img, magnification: int = 2, sensitivities=(1, 2), rad
     if res.shape[2] == 1:
         res = res[:, :, 0]
     return res.cpu().numpy() if from_numpy else res
-
-
-def run_esrrf_parameter_sweep(*args, **kwargs):
-    raise NotImplementedError(
-        "QnR scoring (ErrorMap / FRC / decorrelation) of the parameter sweep is outside this "
-        "engine; esrrf_parameter_sweep() returns the reconstruction grid it scores")
 
 
 class ESRRFAccumulator:

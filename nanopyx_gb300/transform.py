@@ -221,14 +221,15 @@ class eSRRF_ST(LiquidEngine):
         return img.out(out)
 
 
-def _fht_device(t: torch.Tensor, magnification: int) -> torch.Tensor:
-    """(T, H, W) CUDA float32 -> (T, H*m, W*m) Fourier interpolation."""
+def _fht_device(t: torch.Tensor, magnification: int, variant: int = 0) -> torch.Tensor:
+    """(T, H, W) CUDA float32 -> (T, H*m, W*m) Fourier interpolation
+    (variant 0: interpolation.py, 1: _interpolation.pyx)."""
     T, H, W = t.shape
     m = int(magnification)
     out = torch.empty((T, H * m, W * m), dtype=torch.float32, device=t.device)
     if T == 0:
         return out
-    plan = get_fht_plan(H, W, m)
+    plan = get_fht_plan(H, W, m, variant)
     L = N.lib()
     ws = workspace(L.nx_fht_workspace_bytes(plan.handle, T), t.device)
     N.check(L.nx_fht_interpolate(plan.handle, _ptr(t), T, _ptr(out), _ptr(ws), ws.numel(),

@@ -30,6 +30,8 @@ ESRRF_ST_CASES = [
     (8, 1.0, 1, True), (7, 1.5, 1, True), (5, 3.5, 1, True), (2, 0.4, 1, True),
     (4, 1.25, 1.5, True),
 ]
+# scoring: (magnification, radius, sensitivity, ErrorMap fixedSigma)
+SCORE_CASES = [(2, 1.5, 1, 0), (4, 1.0, 2, 0), (2, 2.0, 1, 1)]
 
 
 def main():
@@ -145,7 +147,45 @@ def main():
     g["mpc/input"] = x
     g["mpc/5"] = np.asarray(R["macro_pixel_corrector"](x, magnification=5))
 
-    g = {k: (np.asarray(v, dtype=np.float32) if k != "esrrf_st/cases" else v) for k, v in g.items()}
+    # parameter-sweep scoring (error_map.pyx, frc.pyx, parameter_sweep.py)
+    xd = blinking_stack(1, 24, 20, 6, seed=20)[0]
+    g["score/dht/input"] = xd
+    for mag in (2, 4):
+        g[f"score/dht/{mag}"] = np.asarray(R["dht_interpolation"](xd[None], mag)[0])
+    xs = blinking_stack(20, 32, 32, 12, seed=21)
+    g["score/stack"] = xs
+    ref = np.mean(xs, axis=0)
+    for k, (m, r, s, fixed) in enumerate(SCORE_CASES):
+        rgc = np.asarray(R["eSRRF_ST"](verbose=False).run(xs, magnification=m, radius=r,
+                                                           sensitivity=s, run_type="Threaded"))
+        sr = np.mean(rgc, axis=0)
+        em = R["ErrorMap"]()
+        em.optimise(ref, sr, fixedSigma=fixed)
+        g[f"score/em/{k}/sr"] = sr
+        g[f"score/em/{k}/vals"] = np.array([em.get_sigma(), em._alpha, em._beta, em.getRSE(),
+                                            em.getRSP()], dtype=np.float64)
+        g[f"score/em/{k}/imRSE"] = np.asarray(em.imRSE)
+        odd = np.mean(rgc[1::2], axis=0)
+        even = np.mean(rgc[::2], axis=0)
+        fc = R["FIRECalculator"]()
+        g[f"score/frc/{k}/fire"] = np.array([fc.calculate_fire_number(odd, even)])
+        g[f"score/frc/{k}/odd"] = odd
+        g[f"score/frc/{k}/even"] = even
+    # a non-square, odd-sided pair: the even-square crop
+    a = blinking_stack(2, 37, 44, 10, seed=22)
+    fc = R["FIRECalculator"]()
+    g["score/frc/crop/images"] = a
+    g["score/frc/crop/fire"] = np.array([fc.calculate_fire_number(a[0], a[1])])
+    # the scored sweep: QnR over 2 x 2, all frames and with n_frames slices
+    xq = blinking_stack(10, 32, 32, 12, seed=23)
+    g["score/sweep/input"] = xq
+    g["score/sweep/qnr"] = np.asarray(R["ParameterSweep"]().run(xq, 2, [1, 2], [1.0, 1.5]))
+    g["score/sweep/qnr_nframes4"] = np.asarray(
+        R["ParameterSweep"]().run(xq, 2, [1, 2], [1.0, 1.5], n_frames=4))
+
+    keep64 = ("esrrf_st/cases",)
+    g = {k: (np.asarray(v, dtype=np.float32) if k not in keep64 and "/vals" not in k
+             and not k.startswith("score/sweep/qnr") else np.asarray(v)) for k, v in g.items()}
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT}: {len(g)} arrays, {os.path.getsize(OUT) / 1e6:.2f} MB")
 

@@ -41,8 +41,9 @@ def test_unimplemented_options_raise():
         nx.fht_space_interpolation(np.zeros((2, 4, 4), np.float32), 2, tile_size=128)
     with pytest.raises(NotImplementedError):
         nx.fht_space_interpolation(np.zeros((2, 4, 4), np.float32), 2, doMirrorPadding=False)
+    # the sweep scores by FRC; the decorrelation score is not built
     with pytest.raises(NotImplementedError):
-        nx.run_esrrf_parameter_sweep(np.zeros((2, 4, 4), np.float32))
+        nx.run_esrrf_parameter_sweep(np.zeros((2, 4, 4), np.float32), use_decorr=True)
 
 
 class _Add(LiquidEngine):
@@ -148,3 +149,29 @@ def test_clock_sampler_reads_samples_through_a_pipe():
     with missing:
         pass
     assert missing.summary() is None
+
+
+def test_brent_search_agrees_with_scipy():
+    """The lockstep Brent search finds the minimisers scipy.optimize.brent
+    finds from the same two starting points (including a downhill walk into a
+    flat region, as the error map's blur width takes for sigma <= 0)."""
+    from scipy.optimize import brent
+
+    from nanopyx_gb300.scoring import _lockstep_brent
+
+    fns = [
+        lambda x: (x - 1.3) ** 2 + 0.5,
+        lambda x: np.cos(x) + 0.1 * x,
+        lambda x: np.log1p((x - 4.2) ** 2),
+        lambda x: max(x, 0.0) ** 2 + 1.0,       # flat for x <= 0
+        lambda x: (x - 20.0) ** 2,              # minimum far beyond the bracket
+    ]
+    brack = (0.0, 3.4)
+    got = _lockstep_brent([brack] * len(fns), lambda b: {i: fns[i](x) for i, x in b.items()})
+    for f, g in zip(fns, got):
+        ref = brent(f, brack=brack, maxiter=1000)
+        assert abs(f(g) - f(ref)) <= 1e-12 * max(1.0, abs(f(ref)))
+        if f(-1.0) != f(-2.0):  # a strict minimum: the same abscissa
+            assert abs(g - ref) <= 1e-6 * max(1.0, abs(ref))
+        else:
+            assert g <= 0.0 and ref <= 0.0

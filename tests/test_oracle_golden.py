@@ -126,3 +126,65 @@ def test_compiled_reference_reproduces_golden(golden):
                                                sensitivity=float(s), doIntensityWeighting=bool(iw),
                                                run_type="Threaded")
         assert rel_err(out, golden[f"esrrf_st/{k}"]) <= 1e-5
+
+
+# --- parameter-sweep scoring (oracle/scoring_np.py) ---------------------------
+SCORE_CASES = [(2, 1.5, 1, 0), (4, 1.0, 2, 0), (2, 2.0, 1, 1)]
+
+
+@pytest.mark.parametrize("mag", [2, 4])
+def test_oracle_dht_interpolation(golden, mag):
+    from oracle import scoring_np as S
+
+    got = S.dht_interpolate(golden["score/dht/input"], mag)
+    assert rel_err(got, golden[f"score/dht/{mag}"]) <= 1e-5
+
+
+@pytest.mark.parametrize("k", range(len(SCORE_CASES)))
+def test_oracle_error_map(golden, k):
+    """RSP, RSE and the fit agree with the reference's ErrorMap; the Brent
+    minimum of the (flat) RMSE curve agrees to a few 1e-3."""
+    from oracle import scoring_np as S
+
+    xs = golden["score/stack"]
+    e = S.error_map(np.mean(xs, axis=0), golden[f"score/em/{k}/sr"], SCORE_CASES[k][3])
+    sigma, alpha, beta, rse, rsp = golden[f"score/em/{k}/vals"]
+    assert abs(e["sigma"] - sigma) <= 5e-3 * sigma
+    assert abs(e["alpha"] - alpha) <= 2e-3 * abs(alpha)
+    assert abs(e["beta"] - beta) <= 1e-4 * abs(beta)
+    assert abs(e["rse"] - rse) <= 1e-5 * rse
+    assert abs(e["rsp"] - rsp) <= 1e-5
+    assert rel_err(e["imRSE"], golden[f"score/em/{k}/imRSE"]) <= 1e-3
+
+
+@pytest.mark.parametrize("k", range(len(SCORE_CASES)))
+def test_oracle_fire_number(golden, k):
+    from oracle import scoring_np as S
+
+    f, _ = S.fire_number(golden[f"score/frc/{k}/odd"], golden[f"score/frc/{k}/even"])
+    assert abs(f - golden[f"score/frc/{k}/fire"][0]) <= 1e-5 * f
+
+
+def test_oracle_fire_number_even_square_crop(golden):
+    from oracle import scoring_np as S
+
+    a = golden["score/frc/crop/images"]
+    f, curve = S.fire_number(a[0], a[1])
+    assert curve.shape == (36 // 2 - 1, 3)
+    assert abs(f - golden["score/frc/crop/fire"][0]) <= 1e-5 * f
+
+
+def test_oracle_qnr_of_the_sweep(golden):
+    """The oracle's eSRRF_ST + ErrorMap + FRC + QnR reproduces the reference's
+    ParameterSweep.run on a 2 x 2 grid."""
+    from oracle import scoring_np as S
+
+    xq = golden["score/sweep/input"]
+    rsp = np.zeros((2, 2))
+    frc = np.zeros((2, 2))
+    for si, s in enumerate([1, 2]):
+        for ri, r in enumerate([1.0, 1.5]):
+            rgc = O.esrrf_st(xq, 2, r, s)
+            rsp[si, ri] = S.error_map(np.mean(xq, 0), rgc.mean(0))["rsp"]
+            frc[si, ri] = S.fire_number(rgc[1::2].mean(0), rgc[::2].mean(0))[0]
+    assert np.abs(S.qnr(rsp, frc) - golden["score/sweep/qnr"]).max() <= 1e-5
