@@ -641,7 +641,12 @@ def bench_scored_sweep(dev, repeats=3):
                       "FIRECalculator of one pair (s=2, R=1.5) at 1024x1024",
             "esrrf_st_s_per_frame": t_frame, "error_map_s": t1 - t0, "frc_s": t2 - t1,
             "sweep_s_extrapolated": est,
-            "pair_parity": {"rsp_gpu": em["rsp"][si * 4 + ri], "rsp_reference": emr.getRSP(),
+            # the reference's Pearson correlation sums 1M pixels in float32 per
+            # OpenMP thread: its RSP at this size depends on the thread count
+            "omp_threads": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)),
+            "pair_parity": {"sigma_gpu": em["sigma"][si * 4 + ri],
+                            "sigma_reference": emr.get_sigma(),
+                            "rsp_gpu": em["rsp"][si * 4 + ri], "rsp_reference": emr.getRSP(),
                             "fire_gpu": float(frc[si, ri]), "fire_reference": float(fire_ref)}}
         out["speedup_vs_reference_extrapolated"] = est / t_sweep
     return out

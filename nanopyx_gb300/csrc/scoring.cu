@@ -33,8 +33,7 @@
 namespace nx {
 namespace {
 
-constexpr int kSumBlocks = 256;  // partial-sum blocks of the moment reduction
-constexpr int kSumFields = 6;    // sx, sy, sxx, sxy, syy, s(x-y)^2
+constexpr int kSumFields = 6;    // sx, sy, Sxx, Sxy, Syy, s(x-y)^2
 constexpr int kFftThreads = 256;
 constexpr int kMaxFftN = 8192;   // two complex line buffers in shared memory
 constexpr int kFrcChunk = 8;     // image pairs per FFT launch
@@ -113,43 +112,92 @@ __global__ void gauss_weights_kernel(const __grid_constant__ BlurBatch b, int H,
 }
 
 // axis 0: out[z][y][x] = sum_j w[j] * src[reflect(y + offset + j)][x], the
-// source mapped to alpha * v + beta first when the batch is affine
-__global__ void blur_axis0_kernel(const __grid_constant__ BlurBatch b,
-                                  const float* __restrict__ in, int H, int W,
-                                  const float* __restrict__ w0, float* __restrict__ mid) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+// source mapped to alpha * v + beta first when the batch is affine.  A CTA
+// computes 32 columns x 64 rows (8 rows per thread); with up to kStageTaps
+// taps the weights and the column strip with its reflected halo rows are
+// staged in shared memory, else the taps are read through the cache.
+constexpr int kTileCols = 32, kTileRows = 64, kRowsPerThread = 8;
+constexpr int kStageTaps = 256;
+__global__ void __launch_bounds__(256) blur_axis0_kernel(const __grid_constant__ BlurBatch b,
+                                                         const float* __restrict__ in, int H,
+                                                         int W, const float* __restrict__ w0,
+                                                         int staged, float* __restrict__ mid) {
+  extern __shared__ float sm[];
   const int z = blockIdx.z;
-  if (x >= W || y >= H) return;
+  const int x0 = blockIdx.x * kTileCols, y0 = blockIdx.y * kTileRows;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileCols + tx;
   const float* src = in + (size_t)b.src[z] * H * W;
   const float* w = w0 + (size_t)z * 2 * H;
   const BlurAxis ax = b.ax[0][z];
   const float alpha = b.alpha[z], beta = b.beta[z];
-  float acc = 0.f;
-  for (int j = 0; j < ax.taps; ++j) {
-    long long r = (long long)y + ax.offset + j;
-    if (r < 0 || r >= H) r = reflect_index(r, H);
-    float v = __ldg(src + (size_t)r * W + x);
-    if (b.affine) v = __fadd_rn(__fmul_rn(alpha, v), beta);
-    acc = fmaf(__ldg(w + j), v, acc);
+  const int x = x0 + tx;
+  float acc[kRowsPerThread];
+#pragma unroll
+  for (int q = 0; q < kRowsPerThread; ++q) acc[q] = 0.f;
+  if (staged) {
+    float* ws = sm;
+    float* tile = sm + kStageTaps;
+    for (int k = tid; k < ax.taps; k += 256) ws[k] = w[k];
+    const int rows = kTileRows + ax.taps - 1;
+    for (int idx = tid; idx < rows * kTileCols; idx += 256) {
+      const int k = idx / kTileCols, c = idx % kTileCols;
+      int r = y0 + ax.offset + k;
+      if (r < 0 || r >= H) r = (int)reflect_index(r, H);
+      float v = 0.f;
+      if (x0 + c < W) {
+        v = __ldg(src + (size_t)r * W + x0 + c);
+        if (b.affine) v = __fadd_rn(__fmul_rn(alpha, v), beta);
+      }
+      tile[idx] = v;
+    }
+    __syncthreads();
+    const float* col = tile + ty * kRowsPerThread * kTileCols + tx;
+    for (int j = 0; j < ax.taps; ++j) {
+      const float wj = ws[j];
+#pragma unroll
+      for (int q = 0; q < kRowsPerThread; ++q)
+        acc[q] = fmaf(wj, col[(q + j) * kTileCols], acc[q]);
+    }
+  } else if (x < W) {
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+      const int y = y0 + ty * kRowsPerThread + q;
+      if (y >= H) break;
+      for (int j = 0; j < ax.taps; ++j) {
+        long long r = (long long)y + ax.offset + j;
+        if (r < 0 || r >= H) r = reflect_index(r, H);
+        float v = __ldg(src + (size_t)r * W + x);
+        if (b.affine) v = __fadd_rn(__fmul_rn(alpha, v), beta);
+        acc[q] = fmaf(__ldg(w + j), v, acc[q]);
+      }
+    }
   }
-  mid[((size_t)z * H + y) * W + x] = acc;
+  if (x < W) {
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+      const int y = y0 + ty * kRowsPerThread + q;
+      if (y < H) mid[((size_t)z * H + y) * W + x] = acc[q];
+    }
+  }
 }
 
-// axis 1: the row segment with its reflected halo staged in shared memory
-// when it fits, else read through the cache
+// axis 1: the row segment with its reflected halo (and the weights) staged in
+// shared memory when they fit, else read through the cache
 constexpr int kRowTile = 256;
-__global__ void blur_axis1_kernel(const __grid_constant__ BlurBatch b,
-                                  const float* __restrict__ mid, int H, int W,
-                                  const float* __restrict__ w1, int staged,
-                                  float* __restrict__ out) {
-  extern __shared__ float seg[];
+__global__ void __launch_bounds__(256) blur_axis1_kernel(const __grid_constant__ BlurBatch b,
+                                                         const float* __restrict__ mid, int H,
+                                                         int W, const float* __restrict__ w1,
+                                                         int staged, float* __restrict__ out) {
+  extern __shared__ float sm[];
   const int y = blockIdx.y, z = blockIdx.z;
   const int x0 = blockIdx.x * kRowTile;
   const float* row = mid + ((size_t)z * H + y) * W;
   const float* w = w1 + (size_t)z * 2 * W;
   const BlurAxis ax = b.ax[1][z];
+  float* ws = sm;
+  float* seg = sm + ((ax.taps + 3) & ~3);
   if (staged) {
+    for (int k = threadIdx.x; k < ax.taps; k += blockDim.x) ws[k] = w[k];
     const int span = kRowTile + ax.taps - 1;
     for (int k = threadIdx.x; k < span; k += blockDim.x) {
       long long c = (long long)x0 + ax.offset + k;
@@ -163,7 +211,7 @@ __global__ void blur_axis1_kernel(const __grid_constant__ BlurBatch b,
     if (x >= W) break;
     float acc = 0.f;
     if (staged) {
-      for (int j = 0; j < ax.taps; ++j) acc = fmaf(__ldg(w + j), seg[t + j], acc);
+      for (int j = 0; j < ax.taps; ++j) acc = fmaf(ws[j], seg[t + j], acc);
     } else {
       for (int j = 0; j < ax.taps; ++j) {
         long long c = (long long)x + ax.offset + j;
@@ -176,56 +224,139 @@ __global__ void blur_axis1_kernel(const __grid_constant__ BlurBatch b,
 }
 
 // ---------------------------------------------------------------------------
-// Moment sums of (x, y) pairs, float64
+// Moment sums of (x, y) pairs: sums and centred second moments in float64.
+// FP64 is slow on this GPU, so each thread sums a short run (at most
+// kSumRun elements) in float32 and only the cross-thread reduction is in
+// float64; the second moments are taken about the float32-rounded means
+// (two passes) and corrected to the exact means, so nothing cancels.
 // ---------------------------------------------------------------------------
-__device__ inline void block_sum6(double (&v)[kSumFields], double* red /* [6][blockDim] */) {
-  for (int f = 0; f < kSumFields; ++f) red[f * blockDim.x + threadIdx.x] = v[f];
+constexpr int kSumRun = 8;          // elements per thread and pass (short float32 runs)
+constexpr int kSumMaxBlocks = 2048;
+
+__device__ inline void block_sum(double* v, int nf, double* red /* [nf][blockDim] */) {
+  for (int f = 0; f < nf; ++f) red[f * blockDim.x + threadIdx.x] = v[f];
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s)
-      for (int f = 0; f < kSumFields; ++f)
+      for (int f = 0; f < nf; ++f)
         red[f * blockDim.x + threadIdx.x] += red[f * blockDim.x + threadIdx.x + s];
     __syncthreads();
   }
-  for (int f = 0; f < kSumFields; ++f) v[f] = red[f * blockDim.x];
+  for (int f = 0; f < nf; ++f) v[f] = red[f * blockDim.x];
+  __syncthreads();
 }
 
-__global__ void __launch_bounds__(256) moment_partial_kernel(const float* __restrict__ x,
+// pass 1: sum x, sum y
+__global__ void __launch_bounds__(256) moment_mean_kernel(const float* __restrict__ x,
+                                                          const float* __restrict__ y,
+                                                          long long n,
+                                                          double* __restrict__ part) {
+  __shared__ double red[2 * 256];
+  const float* xs = x + (size_t)blockIdx.y * n;
+  double v[2] = {0, 0};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n;
+       i0 += stride * kSumRun) {
+    float sx = 0.f, sy = 0.f;
+    for (int k = 0; k < kSumRun; ++k) {
+      const long long i = i0 + k * stride;
+      if (i < n) {
+        sx += xs[i];
+        sy += y[i];
+      }
+    }
+    v[0] += sx;
+    v[1] += sy;
+  }
+  block_sum(v, 2, red);
+  if (threadIdx.x == 0) {
+    part[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 2 + 0] = v[0];
+    part[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 2 + 1] = v[1];
+  }
+}
+
+// per image: the two sums in fixed order
+__global__ void __launch_bounds__(256) moment_mean_final_kernel(const double* __restrict__ part,
+                                                                int nparts,
+                                                                double* __restrict__ sums) {
+  __shared__ double red[2 * 256];
+  double v[2] = {0, 0};
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
+    v[0] += part[((size_t)blockIdx.x * nparts + b) * 2 + 0];
+    v[1] += part[((size_t)blockIdx.x * nparts + b) * 2 + 1];
+  }
+  block_sum(v, 2, red);
+  if (threadIdx.x == 0) {
+    sums[blockIdx.x * 2 + 0] = v[0];
+    sums[blockIdx.x * 2 + 1] = v[1];
+  }
+}
+
+// pass 2: products about the float32-rounded means, and (x - y)^2
+__global__ void __launch_bounds__(256) moment_centred_kernel(const float* __restrict__ x,
                                                              const float* __restrict__ y,
                                                              long long n,
+                                                             const double* __restrict__ sums,
                                                              double* __restrict__ part) {
-  __shared__ double red[kSumFields * 256];
+  __shared__ double red[4 * 256];
   const int z = blockIdx.y;
   const float* xs = x + (size_t)z * n;
-  const float* ys = y;  // the second image is shared by the batch
-  double v[kSumFields] = {0, 0, 0, 0, 0, 0};
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const double a = xs[i], b = ys[i];
-    const double d = (double)__fsub_rn(xs[i], ys[i]);
-    v[0] += a;
-    v[1] += b;
-    v[2] += a * a;
-    v[3] += a * b;
-    v[4] += b * b;
-    v[5] += d * d;
+  const float mx = (float)(sums[2 * z] / (double)n), my = (float)(sums[2 * z + 1] / (double)n);
+  double v[4] = {0, 0, 0, 0};
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n;
+       i0 += stride * kSumRun) {
+    float cxx = 0.f, cxy = 0.f, cyy = 0.f, dd = 0.f;
+    for (int k = 0; k < kSumRun; ++k) {
+      const long long i = i0 + k * stride;
+      if (i < n) {
+        const float a = xs[i], b = y[i];
+        const float dx = a - mx, dy = b - my, d = __fsub_rn(a, b);
+        cxx = fmaf(dx, dx, cxx);
+        cxy = fmaf(dx, dy, cxy);
+        cyy = fmaf(dy, dy, cyy);
+        dd = fmaf(d, d, dd);
+      }
+    }
+    v[0] += cxx;
+    v[1] += cxy;
+    v[2] += cyy;
+    v[3] += dd;
   }
-  block_sum6(v, red);
+  block_sum(v, 4, red);
   if (threadIdx.x == 0)
-    for (int f = 0; f < kSumFields; ++f)
-      part[((size_t)z * gridDim.x + blockIdx.x) * kSumFields + f] = v[f];
+    for (int f = 0; f < 4; ++f) part[((size_t)z * gridDim.x + blockIdx.x) * 4 + f] = v[f];
 }
 
+// per image: (sum x, sum y, Sxx, Sxy, Syy, sum (x-y)^2), S centred about the
+// exact means: S(x - m~) = S(x - m) + n (m - m~)(...)
 __global__ void __launch_bounds__(256) moment_final_kernel(const double* __restrict__ part,
-                                                           int nparts, double* __restrict__ out) {
-  __shared__ double red[kSumFields * 256];
+                                                           int nparts, long long n,
+                                                           const double* __restrict__ sums,
+                                                           double* __restrict__ out) {
+  __shared__ double red[4 * 256];
   const int z = blockIdx.x;
-  double v[kSumFields] = {0, 0, 0, 0, 0, 0};
+  double v[4] = {0, 0, 0, 0};
   for (int b = threadIdx.x; b < nparts; b += blockDim.x)
-    for (int f = 0; f < kSumFields; ++f) v[f] += part[((size_t)z * nparts + b) * kSumFields + f];
-  block_sum6(v, red);
-  if (threadIdx.x == 0)
-    for (int f = 0; f < kSumFields; ++f) out[(size_t)z * kSumFields + f] = v[f];
+    for (int f = 0; f < 4; ++f) v[f] += part[((size_t)z * nparts + b) * 4 + f];
+  block_sum(v, 4, red);
+  if (threadIdx.x == 0) {
+    const double sx = sums[2 * z], sy = sums[2 * z + 1];
+    const double ex = sx / (double)n, ey = sy / (double)n;
+    const double ox = ex - (double)(float)ex, oy = ey - (double)(float)ey;
+    double* o = out + (size_t)z * kSumFields;
+    o[0] = sx;
+    o[1] = sy;
+    o[2] = v[0] - (double)n * ox * ox;
+    o[3] = v[1] - (double)n * ox * oy;
+    o[4] = v[2] - (double)n * oy * oy;
+    o[5] = v[3];
+  }
+}
+
+int sum_blocks(long long n) {
+  return (int)std::max<long long>(
+      1, std::min<long long>(kSumMaxBlocks, (n + 256LL * kSumRun - 1) / (256LL * kSumRun)));
 }
 
 // ---------------------------------------------------------------------------
@@ -368,7 +499,7 @@ __global__ void __launch_bounds__(256) frc_ring_kernel(const float2* __restrict_
       v[f] += (double)__fadd_rn(lo, __fmul_rn(fy, __fsub_rn(up, lo)));
     }
   }
-  block_sum6(v, red);
+  block_sum(v, 3, red);
   if (threadIdx.x == 0) {
     sums[(size_t)r * 4 + 0] = v[0];
     sums[(size_t)r * 4 + 1] = v[1];
@@ -516,13 +647,21 @@ int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* sr
     }
     gauss_weights_kernel<<<dim3(b.n, 2), 256, 0, s>>>(b, H, W, w0, w1);
     NX_CUDA_TRY(cudaGetLastError());
-    blur_axis0_kernel<<<dim3((W + 31) / 32, (H + 7) / 8, b.n), dim3(32, 8), 0, s>>>(
-        b, d_in, H, W, w0, mid);
+    int max_taps0 = 1;
+    for (int i = 0; i < b.n; ++i) max_taps0 = std::max(max_taps0, b.ax[0][i].taps);
+    const int staged0 = max_taps0 <= kStageTaps;
+    const size_t smem0 =
+        staged0 ? (kStageTaps + (size_t)(kTileRows + max_taps0 - 1) * kTileCols) * sizeof(float)
+                : 0;
+    blur_axis0_kernel<<<dim3((W + kTileCols - 1) / kTileCols, (H + kTileRows - 1) / kTileRows,
+                             b.n),
+                        dim3(kTileCols, 256 / kTileCols), smem0, s>>>(b, d_in, H, W, w0, staged0,
+                                                                      mid);
     NX_CUDA_TRY(cudaGetLastError());
-    const size_t seg = ((size_t)kRowTile + max_taps1 - 1) * sizeof(float);
-    const int staged = seg <= 48 * 1024;
-    blur_axis1_kernel<<<dim3((W + kRowTile - 1) / kRowTile, H, b.n), 256, staged ? seg : 0, s>>>(
-        b, mid, H, W, w1, staged, d_out + (size_t)c0 * plane);
+    const size_t smem1 = (((size_t)max_taps1 + 3) / 4 * 4 + kRowTile + max_taps1 - 1) * sizeof(float);
+    const int staged1 = smem1 <= 48 * 1024;
+    blur_axis1_kernel<<<dim3((W + kRowTile - 1) / kRowTile, H, b.n), 256, staged1 ? smem1 : 0,
+                        s>>>(b, mid, H, W, w1, staged1, d_out + (size_t)c0 * plane);
     NX_CUDA_TRY(cudaGetLastError());
   }
   return NX_OK;
@@ -540,7 +679,8 @@ int nx_gaussian_blur(const float* d_in, int H, int W, double sigma, int affine, 
 }
 
 size_t nx_moment_sums_workspace_bytes(int batch) {
-  return 256 + (size_t)std::max(batch, 1) * kSumBlocks * kSumFields * sizeof(double);
+  const size_t b = (size_t)std::max(batch, 1);
+  return 256 + b * kSumMaxBlocks * 4 * sizeof(double) + b * 2 * sizeof(double);
 }
 
 int nx_moment_sums(const float* d_x, const float* d_y, long long n, int batch, double* d_sums,
@@ -553,10 +693,16 @@ int nx_moment_sums(const float* d_x, const float* d_y, long long n, int batch, d
     return NX_ERR_WORKSPACE;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  double* part = (double*)((char*)d_ws + 256);
-  moment_partial_kernel<<<dim3(kSumBlocks, batch), 256, 0, s>>>(d_x, d_y, n, part);
+  double* part = (double*)((char*)d_ws + 256);                    // batch x blocks x 4
+  double* means = part + (size_t)batch * kSumMaxBlocks * 4;       // batch x 2 (the sums)
+  const int nb = sum_blocks(n);
+  moment_mean_kernel<<<dim3(nb, batch), 256, 0, s>>>(d_x, d_y, n, part);
   NX_CUDA_TRY(cudaGetLastError());
-  moment_final_kernel<<<batch, 256, 0, s>>>(part, kSumBlocks, d_sums);
+  moment_mean_final_kernel<<<batch, 256, 0, s>>>(part, nb, means);
+  NX_CUDA_TRY(cudaGetLastError());
+  moment_centred_kernel<<<dim3(nb, batch), 256, 0, s>>>(d_x, d_y, n, means, part);
+  NX_CUDA_TRY(cudaGetLastError());
+  moment_final_kernel<<<batch, 256, 0, s>>>(part, nb, n, means, d_sums);
   NX_CUDA_TRY(cudaGetLastError());
   return NX_OK;
 }

@@ -77,8 +77,9 @@ def gaussian_blur(img: torch.Tensor, sigma: float, alpha: float | None = None,
 
 
 def moment_sums(x: torch.Tensor, y: torch.Tensor) -> np.ndarray:
-    """float64 (sum x, sum y, sum x^2, sum xy, sum y^2, sum (x-y)^2) of each
-    image of ``x`` ((B, n) or (n,)) against ``y`` (n,); returns (B, 6) on the host."""
+    """float64 moments of each image of ``x`` ((B, n) or (n,)) against ``y``
+    (n,): (sum x, sum y, Sxx, Sxy, Syy, sum (x-y)^2) with S the second moments
+    about the means; returns (B, 6) on the host."""
     xs = x.reshape(-1, y.numel())
     B = xs.shape[0]
     L = N.lib()
@@ -90,28 +91,22 @@ def moment_sums(x: torch.Tensor, y: torch.Tensor) -> np.ndarray:
 
 
 def _pearson(s, n: int) -> float:
-    """Pearson correlation from moment sums; 0 where a variance vanishes
+    """Pearson correlation from the moments; 0 where a variance vanishes
     (pearson_correlation.pyx:60-77)."""
-    sx, sy, sxx, sxy, syy = s[:5]
-    cxx = sxx - sx * sx / n
-    cyy = syy - sy * sy / n
-    cxy = sxy - sx * sy / n
+    cxx, cxy, cyy = s[2], s[3], s[4]
     if cxx <= 0 or cyy <= 0:
         return 0.0
     return float(np.float32(cxy / np.sqrt(cxx * cyy)))
 
 
 def _regression(s, n: int):
-    """scipy.stats.linregress(x, y) slope and intercept from moment sums, and
+    """scipy.stats.linregress(x, y) slope and intercept from the moments, and
     the RMSE of ``slope * x + intercept`` against y."""
-    sx, sy, sxx, sxy, syy = s[:5]
-    mx, my = sx / n, sy / n
-    cxx = sxx - sx * mx
-    cxy = sxy - sx * my
-    cyy = syy - sy * my
+    mx, my = s[0] / n, s[1] / n
+    cxx, cxy, cyy = s[2], s[3], s[4]
     slope = cxy / cxx if cxx != 0 else np.nan
     intercept = my - slope * mx
-    resid = cyy - 2 * slope * cxy + slope * slope * cxx + n * (my - slope * mx - intercept) ** 2
+    resid = cyy - 2 * slope * cxy + slope * slope * cxx
     return slope, intercept, float(np.sqrt(max(resid, 0.0) / n))
 
 
@@ -749,3 +744,29 @@ def run_esrrf_parameter_sweep(img, magnification: int = 2, sensitivities: list =
         return out
     sens_idx, rad_idx = np.unravel_index(np.argmax(out), out.shape)
     return sensitivities[sens_idx], radii[rad_idx]
+
+
+def calculate_error_map(img_ref, img_sr):
+    """(error map, RSE, RSP) of a super-resolution image against its reference
+    (methods/squirrel/error_map.py:5-36)."""
+    em = ErrorMap()
+    em.optimise(img_ref, img_sr)
+    rse_map = em.imRSE
+    if isinstance(rse_map, torch.Tensor):
+        rse_map = rse_map.cpu().numpy()
+    return np.asarray(rse_map, dtype=np.float32), em.getRSE(), em.getRSP()
+
+
+def calculate_frc(frame_1, frame_2, pixel_size: float = 1, units: str = "pixel",
+                  plot_frc_curve: bool = False):
+    """FRC resolution of two frames (methods/squirrel/resolution.py:7-44)."""
+    fc = FIRECalculator(pixel_size=pixel_size, units=units)
+    res = fc.calculate_fire_number(frame_1, frame_2)
+    if plot_frc_curve:
+        from matplotlib import pyplot as plt
+
+        plt.axis("off")
+        plt.subplots_adjust(left=0, right=1, top=1, bottom=0, wspace=0, hspace=0)
+        plt.imshow(fc.plot_frc_curve())
+        plt.show()
+    return res

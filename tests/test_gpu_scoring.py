@@ -65,8 +65,17 @@ def test_moment_sums_match_float64():
     for b in range(3):
         a, c = x[b].ravel().astype(np.float64), y.ravel().astype(np.float64)
         d = (x[b] - y).ravel().astype(np.float64)
-        ref = [a.sum(), c.sum(), (a * a).sum(), (a * c).sum(), (c * c).sum(), (d * d).sum()]
-        assert np.allclose(got[b], ref, rtol=1e-12, atol=0)
+        da, dc = a - a.mean(), c - c.mean()
+        ref = [a.sum(), c.sum(), (da * da).sum(), (da * dc).sum(), (dc * dc).sum(), (d * d).sum()]
+        assert np.allclose(got[b][:2], ref[:2], rtol=1e-9, atol=0)
+        assert np.allclose(got[b][2:], ref[2:], rtol=1e-6, atol=0)
+    # a large offset and a small spread: the centred moments do not cancel
+    z = (1000.0 + rng.standard_normal(1 << 20) * 0.01).astype(np.float32)
+    w = (z + rng.standard_normal(1 << 20).astype(np.float32) * 0.01).astype(np.float32)
+    got = scoring.moment_sums(torch.from_numpy(z).cuda(), torch.from_numpy(w).cuda())[0]
+    a, c = z.astype(np.float64), w.astype(np.float64)
+    da, dc = a - a.mean(), c - c.mean()
+    assert np.allclose(got[2:5], [(da * da).sum(), (da * dc).sum(), (dc * dc).sum()], rtol=1e-5)
 
 
 @pytest.mark.parametrize("n", [26, 36, 200, 256, 1280])
