@@ -277,6 +277,22 @@ size_t nx_fht_workspace_bytes(const nx_fht_plan* plan, int T);
 int nx_fht_interpolate(const nx_fht_plan* plan, const float* d_in, int T, float* d_out, void* d_ws,
                        size_t ws_bytes, void* stream);
 
+/* eSRRF-3D of a (T, S, H, W) stack into d_out (S*mz, H*mxy, W*mxy): per frame
+ * the 3-D gradients, Catmull-Rom x mxy in every slice (slices repeated mz
+ * times, as the reference's z step does), the 3-D RGC inside the margins to
+ * the power `sensitivity`, times the intensity when do_intensity_weighting;
+ * then the frames' mean (mode 0) or standard deviation (mode 1).  radius_z =
+ * radius * PSF_ratio / voxel_ratio.  Voxels outside the margins are 0.
+ *   src/nanopyx/core/transform/_le_esrrf3d.pyx:35-140
+ *   src/include/_c_sr_radial_gradient_convergence.c:92-204
+ *   src/include/_c_gradients.c:75-116                                        */
+size_t nx_esrrf3d_workspace_bytes(int S, int H, int W, int magnification_xy,
+                                  int magnification_z, int mode);
+int nx_esrrf3d_st(const float* d_in, int T, int S, int H, int W, int magnification_xy,
+                  int magnification_z, double radius, double radius_z, float sensitivity,
+                  int mode, int do_intensity_weighting, float* d_out, void* d_ws,
+                  size_t ws_bytes, void* stream);
+
 /* Parameter-sweep scoring (src/nanopyx/core/analysis/parameter_sweep.py:99-139).
  *
  * Gaussian blur with scipy.ndimage.gaussian_filter's definition, as ErrorMap

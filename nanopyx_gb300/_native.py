@@ -98,6 +98,9 @@ _SIGS = {
     "nx_fht_plan_destroy": (_I, [_P]),
     "nx_fht_workspace_bytes": (_SZ, [_P, _I]),
     "nx_fht_interpolate": (_I, [_P, _P, _I, _P, _P, _SZ, _P]),
+    "nx_esrrf3d_workspace_bytes": (_SZ, [_I, _I, _I, _I, _I, _I]),
+    "nx_esrrf3d_st": (_I, [_P, _I, _I, _I, _I, _I, _I, C.c_double, C.c_double, C.c_float, _I, _I,
+                           _P, _P, _SZ, _P]),
     "nx_gaussian_blur_workspace_bytes": (_SZ, [_I, _I]),
     "nx_gaussian_blur": (_I, [_P, _I, _I, C.c_double, _I, C.c_float, C.c_float, _P, _P, _SZ, _P]),
     "nx_gaussian_blur_batch_workspace_bytes": (_SZ, [_I, _I, _I]),

@@ -24,7 +24,7 @@ from ._device import check_image, get_plan, stream_ptr, to_device_stack, workspa
 from .transform import (GradientRobertsCross, Radiality, ShiftAndMagnify,  # noqa: F401
                         macro_pixel_corrector)
 
-__all__ = ["eSRRF", "SRRF", "Workflow", "ESRRFAccumulator", "esrrf_parameter_sweep",
+__all__ = ["eSRRF", "eSRRF3D", "SRRF", "Workflow", "ESRRFAccumulator", "esrrf_parameter_sweep",
            "esrrf_device"]
 
 
@@ -403,3 +403,36 @@ class ESRRFAccumulator:
         N.check(N.lib().nx_workspace_status(self._ws.data_ptr(), stream_ptr()), "eSRRF")
         res = out.cpu().numpy()
         return res[0] if isinstance(temporal_correlation, str) else tuple(res)
+
+
+def eSRRF3D(img, magnification_xy=2, magnification_z=2, radius: float = 1.5,
+            PSF_ratio: float = 2.8, voxel_ratio: float = 4.0, sensitivity: float = 1,
+            frames_per_timepoint: int = 0, mode: str = "average", doIntensityWeighting: bool = True,
+            macro_pixel_correction: bool = True, _force_run_type=None):
+    """eSRRF-3D of a (T, S, H, W) stack (methods/esrrf_3d/eSRRF3D_workflow.py:8-107):
+    per timepoint of ``frames_per_timepoint`` frames an eSRRF3D_ST volume
+    (S*mz, H*mxy, W*mxy), macro-pixel corrected slice by slice; returns
+    (n_timepoints, S*mz, H*mxy, W*mxy) float32 (NumPy in, NumPy out; CUDA
+    tensor in, CUDA tensor out)."""
+    from .transform import eSRRF3D_ST, macro_pixel_corrector
+
+    T = img.shape[0]
+    if frames_per_timepoint == 0 or frames_per_timepoint > T:
+        frames_per_timepoint = T
+    n_tp = T // frames_per_timepoint + (1 if T % frames_per_timepoint else 0)
+    on_dev = isinstance(img, torch.Tensor) and img.is_cuda
+    outs = []
+    for i in range(n_tp):
+        v = eSRRF3D_ST(verbose=False).run(
+            img[frames_per_timepoint * i:frames_per_timepoint * (i + 1)],
+            magnification_xy=magnification_xy, magnification_z=magnification_z, radius=radius,
+            PSF_ratio=PSF_ratio, voxel_ratio=voxel_ratio, sensitivity=sensitivity, mode=mode,
+            doIntensityWeighting=doIntensityWeighting)
+        if v is None:
+            raise ValueError("eSRRF3D: radius or radius_z too large for the volume")
+        if macro_pixel_correction:
+            v = macro_pixel_corrector(v, magnification=magnification_xy)
+        outs.append(v)
+    if on_dev:
+        return torch.stack([o if isinstance(o, torch.Tensor) else torch.as_tensor(o) for o in outs])
+    return np.stack([np.asarray(o, dtype=np.float32) for o in outs]).astype(np.float32)

@@ -359,3 +359,62 @@ def macro_pixel_corrector(img, magnification: int):
                                            stream_ptr()),
             "macro_pixel_corrector")
     return t.cpu().numpy() if src_np else t
+
+
+class eSRRF3D_ST(LiquidEngine):
+    """eSRRF-3D single task (``_le_esrrf3d.pyx:26-140``): a (T, S, H, W) stack
+    (or one (S, H, W) volume) -> (S*mz, H*mxy, W*mxy), the frames' RGC-3D
+    mean (``mode="average"``) or standard deviation (``mode="std"``).  Like the
+    reference, an oversized radius prints a warning and returns None."""
+
+    _designation = "eSRRF_3D"
+
+    def run(self, image, magnification_xy: int = 2, magnification_z: int = 2,
+            radius: float = 1.5, PSF_ratio: float = 2.8, voxel_ratio: float = 4.0,
+            sensitivity: float = 1, mode: str = "average", doIntensityWeighting: bool = True,
+            run_type=None):
+        radius_z = radius * PSF_ratio / voxel_ratio
+        shape = tuple(image.shape)
+        if len(shape) == 3:
+            shape = (1,) + shape
+        if len(shape) != 4:
+            print("Warning:image must either be 3D or 4D. If 3D, it will be reshaped to 4D.")
+            return None
+        if radius > shape[2] / 2 or radius * 2 > shape[3] / 2:
+            print("Warning: Radius is too big for the image. The radius must be smaller than "
+                  "half the number of columns and half number of rows of the image.")
+            return None
+        if radius_z > shape[1] / 2:
+            print("Warning: Radius_z is too big for the image. The radius_z must be smaller "
+                  "than half of number of Z planes. Radius_z is automatically calculated from "
+                  "radius * PSF_ratio / voxel_ratio.")
+            return None
+        if mode not in ("average", "std"):
+            raise ValueError("mode must be 'average' or 'std'")
+        return self._run(image, magnification_xy=magnification_xy,
+                         magnification_z=magnification_z, radius=radius, radius_z=radius_z,
+                         sensitivity=sensitivity, mode=mode,
+                         doIntensityWeighting=doIntensityWeighting, run_type=run_type)
+
+    def _run_cuda(self, image, magnification_xy=2, magnification_z=2, radius=1.5, radius_z=1.05,
+                  sensitivity=1, mode="average", doIntensityWeighting=True):
+        if isinstance(image, torch.Tensor):
+            t = image.to(torch.float32)
+            from_np = not t.is_cuda
+            t = t.to(require_cuda()).contiguous()
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(image, dtype=np.float32))).to(
+                require_cuda())
+            from_np = True
+        if t.ndim == 3:
+            t = t[None]
+        T, S, H, W = t.shape
+        mxy, mz = int(magnification_xy), int(magnification_z)
+        out = torch.empty((S * mz, H * mxy, W * mxy), dtype=torch.float32, device=t.device)
+        md = 1 if mode == "std" else 0
+        L = N.lib()
+        ws = workspace(L.nx_esrrf3d_workspace_bytes(S, H, W, mxy, mz, md), t.device)
+        N.check(L.nx_esrrf3d_st(_ptr(t), T, S, H, W, mxy, mz, float(radius), float(radius_z),
+                                float(sensitivity), md, 1 if doIntensityWeighting else 0,
+                                _ptr(out), _ptr(ws), ws.numel(), stream_ptr()), "eSRRF3D")
+        return out.cpu().numpy() if from_np else out

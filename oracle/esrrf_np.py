@@ -584,3 +584,153 @@ def srrf(stack, magnification=5, ringRadius=0.5, border=0, radialityPositivityCo
     if macro_pixel_correction:
         rad = macro_pixel_correct(rad, magnification)
     return rad
+
+
+# ---------------------------------------------------------------------------
+# eSRRF-3D (src/nanopyx/core/transform/_le_esrrf3d.pyx:65-140,
+# src/nanopyx/core/transform/_interpolation.pyx:54-104,
+# src/include/_c_gradients.c:75-116,
+# src/include/_c_sr_radial_gradient_convergence.c:92-204,
+# src/nanopyx/methods/esrrf_3d/eSRRF3D_workflow.py:8-107)
+# ---------------------------------------------------------------------------
+def interpolate_3d_zlinear(vol, mxy, mz):
+    """Catmull-Rom x mxy in every slice, then the slices repeated mz times:
+    the reference's "linear" z step takes slice sM // mz with weight 1 (its
+    slice coordinate is an integer division)."""
+    v = np.asarray(vol, dtype=np.float64)
+    if mxy > 1:
+        v = cr_shift_magnify(v, 0, 0, mxy, mxy)
+    if mz > 1:
+        v = np.repeat(v, mz, axis=0)
+    return v
+
+
+def gradient_3d(vol):
+    """Central differences along x and y, the backward difference along z,
+    halved, with indices clamped to the volume."""
+    v = np.asarray(vol, dtype=np.float64)
+    S, H, W = v.shape
+    zi, yi, xi = np.arange(S), np.arange(H), np.arange(W)
+    zm = np.maximum(zi - 1, 0)
+    yp, ym = np.minimum(yi + 1, H - 1), np.maximum(yi - 1, 0)
+    xp, xm = np.minimum(xi + 1, W - 1), np.maximum(xi - 1, 0)
+    gc = (v[:, :, xp] - v[:, :, xm]) / 2
+    gr = (v[:, yp, :] - v[:, ym, :]) / 2
+    gs = (v - v[zm]) / 2
+    return gc, gr, gs
+
+
+def rgc3d_params(radius, radius_z):
+    f32 = np.float32
+    sigma = f32(radius / 2.355)
+    sigma_z = f32(radius_z / 2.355)
+    return dict(tSS=f32(f32(2) * sigma * sigma), tSO=f32(f32(2) * sigma + f32(1)),
+                tSS_z=f32(f32(2) * sigma_z * sigma_z), tSO_z=f32(f32(2) * sigma_z + f32(1)),
+                fwhm=f32(radius), fwhm_z=f32(radius_z))
+
+
+def rgc3d_frame(gc, gr, gs, S, H, W, mxy, mz, radius, radius_z, sensitivity):
+    """RGC-3D of one frame at every output voxel inside the margins (float64
+    weights and sums; sample geometry and gradient indices in float32 as the
+    reference forms them)."""
+    f32 = np.float32
+    p = rgc3d_params(radius, radius_z)
+    Sm, Hm, Wm = S * mz, H * mxy, W * mxy
+    margin = int(radius * mxy)
+    margin_z = int(radius_z * mz)
+    out = np.zeros((Sm, Hm, Wm))
+    sM, rM, cM = np.meshgrid(np.arange(margin_z, Sm - margin_z), np.arange(margin, Hm - margin),
+                             np.arange(margin, Wm - margin), indexing="ij")
+    if sM.size == 0:
+        return out
+    xc = (cM.astype(f32) / f32(mxy)).astype(f32)
+    yc = (rM.astype(f32) / f32(mxy)).astype(f32)
+    zc = (sM.astype(f32) / f32(mz)).astype(f32)
+    rgc = np.zeros(sM.shape)
+    wsum = np.zeros(sM.shape)
+    s0, s1 = -int(p["fwhm"]), int(p["fwhm"] + f32(1))
+    z0, z1 = -int(p["fwhm_z"]), int(p["fwhm_z"] + f32(1))
+    tSS, tSS_z = float(p["tSS"]), float(p["tSS_z"])
+    for j in range(s0, s1 + 1):
+        vy = (yc + f32(j)).astype(f32)
+        for i in range(s0, s1 + 1):
+            vx = (xc + f32(i)).astype(f32)
+            for k in range(z0, z1 + 1):
+                vz = (zc + f32(k)).astype(f32)
+                ok = (vy > 0) & (vy <= H - 1) & (vx > 0) & (vx <= W - 1) & (vz > 0) & (vz <= S - 1)
+                dx = (vx - xc).astype(f32)
+                dy = (vy - yc).astype(f32)
+                dz = (vz - zc).astype(f32)
+                dxy2 = (dx * dx + dy * dy).astype(f32)
+                dist = np.sqrt((dxy2 + dz * dz).astype(f32).astype(np.float64)).astype(f32)
+                dxy = np.sqrt(dxy2.astype(np.float64)).astype(f32)
+                ok &= (dist != 0) & (dxy <= p["tSO"]) & (dz <= p["tSO_z"])
+                if not ok.any():
+                    continue
+                zi = (vz * f32(mz)).astype(f32).astype(np.int64)
+                yi = (f32(mxy) * vy).astype(f32).astype(np.int64)
+                xi = (f32(mxy) * vx).astype(f32).astype(np.int64)
+                zi, yi, xi = (np.where(ok, a, 0) for a in (zi, yi, xi))
+                Gx, Gy, Gz = gc[zi, yi, xi], gr[zi, yi, xi], gs[zi, yi, xi]
+                d, x_, y_, z_ = (a.astype(np.float64) for a in (dist, dx, dy, dz))
+                w = (d * np.exp(-x_ * x_ / tSS - y_ * y_ / tSS) * np.exp(-z_ * z_ / tSS_z)) ** 4
+                w = np.where(ok, w, 0.0)
+                wsum += w
+                gdr = Gx * x_ + Gy * y_ + Gz * z_
+                c1, c2, c3 = Gy * z_ - Gz * y_, Gz * x_ - Gx * z_, Gx * y_ - Gy * x_
+                gm = np.sqrt(Gx * Gx + Gy * Gy + Gz * Gz)
+                with np.errstate(invalid="ignore", divide="ignore"):
+                    dk = np.sqrt(c1 * c1 + c2 * c2 + c3 * c3) / gm
+                dk = np.where(np.isnan(dk), d, dk)
+                dk = 1 - dk / d
+                rgc += np.where(ok & (gdr < 0), dk * w, 0.0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rgc = rgc / wsum
+    if sensitivity > 1:
+        rgc = np.where(rgc >= 0, np.abs(rgc) ** sensitivity, rgc)
+    rgc = np.where(rgc < 0, 0.0, rgc)
+    out[margin_z:Sm - margin_z, margin:Hm - margin, margin:Wm - margin] = rgc
+    return out
+
+
+def esrrf3d_st(stack, magnification_xy=2, magnification_z=2, radius=1.5, PSF_ratio=2.8,
+               voxel_ratio=4.0, sensitivity=1, mode="average", doIntensityWeighting=True):
+    """eSRRF3D_ST.run on a (T, S, H, W) stack: per frame RGC-3D (times the
+    interpolated intensity), then the frames' mean or standard deviation."""
+    x = np.asarray(stack, dtype=np.float32)
+    if x.ndim == 3:
+        x = x[None]
+    radius_z = radius * PSF_ratio / voxel_ratio
+    T, S, H, W = x.shape
+    mxy, mz = magnification_xy, magnification_z
+    maps = []
+    for f in range(T):
+        v = x[f]
+        g = gradient_3d(v)
+        gm = [interpolate_3d_zlinear(a.astype(np.float32), mxy, mz) for a in g]
+        r = rgc3d_frame(*gm, S, H, W, mxy, mz, radius, radius_z, sensitivity)
+        if doIntensityWeighting:
+            r = r * interpolate_3d_zlinear(v, mxy, mz)
+        maps.append(r)
+    maps = np.stack(maps)
+    if mode == "std":
+        return np.sqrt(maps.var(axis=0))
+    return maps.mean(axis=0)
+
+
+def esrrf3d(stack, magnification_xy=2, magnification_z=2, radius=1.5, PSF_ratio=2.8,
+            voxel_ratio=4.0, sensitivity=1, frames_per_timepoint=0, mode="average",
+            doIntensityWeighting=True, macro_pixel_correction=True):
+    """The eSRRF3D workflow: per timepoint eSRRF3D_ST, then the per-slice
+    macro-pixel correction; (n_tp, S*mz, H*mxy, W*mxy)."""
+    x = np.asarray(stack, dtype=np.float32)
+    T = x.shape[0]
+    fpt = T if frames_per_timepoint == 0 or frames_per_timepoint > T else frames_per_timepoint
+    outs = []
+    for t0 in range(0, T, fpt):
+        v = esrrf3d_st(x[t0:t0 + fpt], magnification_xy, magnification_z, radius, PSF_ratio,
+                       voxel_ratio, sensitivity, mode, doIntensityWeighting)
+        if macro_pixel_correction:
+            v = macro_pixel_correct(v, magnification_xy)
+        outs.append(v)
+    return np.stack(outs)

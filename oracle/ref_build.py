@@ -33,6 +33,7 @@ Reference files used (paths inside the reference project):
     src/nanopyx/core/transform/_le_radial_gradient_convergence.pyx
     src/nanopyx/core/transform/_le_radiality.pyx
     src/nanopyx/core/transform/mpcorrector.pyx
+    src/nanopyx/core/transform/_le_esrrf3d.pyx
     src/nanopyx/core/transform/{_interpolation,error_map,edges,normalize}.pyx
     src/nanopyx/core/transform/{__interpolation_tools__,interpolation,
                                 sr_temporal_correlations,padding}.py
@@ -72,6 +73,8 @@ PYX_SPECS = [
     ("transform", "_le_radiality", ["_c_sr_radiality", "_c_interpolation_catmull_rom", "_c_gradients"]),
     ("transform", "_le_esrrf", []),
     ("transform", "mpcorrector", []),
+    # eSRRF-3D
+    ("transform", "_le_esrrf3d", ["_c_gradients", "_c_sr_radial_gradient_convergence"]),
     # the parameter sweep's scoring: ErrorMap (RSP), FIRECalculator (FRC),
     # DecorrAnalysis and what they cimport
     ("transform", "_interpolation", ["_c_interpolation_catmull_rom"]),
@@ -290,6 +293,7 @@ def load():
         "DecorrAnalysis": mods["decorr"].DecorrAnalysis,
         "ParameterSweep": mods["parameter_sweep"].ParameterSweep,
         "pearson_correlation": mods["pearson_correlation"].pearson_correlation,
+        "eSRRF3D_ST": mods["_le_esrrf3d"].eSRRF3D,
     }
 
 

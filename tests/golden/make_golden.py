@@ -30,6 +30,9 @@ ESRRF_ST_CASES = [
     (8, 1.0, 1, True), (7, 1.5, 1, True), (5, 3.5, 1, True), (2, 0.4, 1, True),
     (4, 1.25, 1.5, True),
 ]
+# eSRRF-3D: (magnification_xy, magnification_z, radius, sensitivity, mode, intensity weighting)
+ESRRF3D_CASES = [(2, 2, 1.5, 1, "average", 1), (3, 1, 1.0, 2, "std", 1), (2, 3, 2.0, 1, "average", 0),
+                 (1, 2, 1.5, 1, "average", 1)]
 # scoring: (magnification, radius, sensitivity, ErrorMap fixedSigma)
 SCORE_CASES = [(2, 1.5, 1, 0), (4, 1.0, 2, 0), (2, 2.0, 1, 1)]
 
@@ -182,6 +185,22 @@ def main():
     g["score/sweep/qnr"] = np.asarray(R["ParameterSweep"]().run(xq, 2, [1, 2], [1.0, 1.5]))
     g["score/sweep/qnr_nframes4"] = np.asarray(
         R["ParameterSweep"]().run(xq, 2, [1, 2], [1.0, 1.5], n_frames=4))
+
+    # eSRRF-3D (_le_esrrf3d.pyx, eSRRF3D_workflow.py)
+    x3 = (np.random.default_rng(24).random((5, 6, 14, 12)) * 100 + 10).astype(np.float32)
+    g["esrrf3d/input"] = x3
+    for k, (mxy, mz, r, s, mode, iw) in enumerate(ESRRF3D_CASES):
+        g[f"esrrf3d/{k}"] = np.asarray(R["eSRRF3D_ST"](verbose=False).run(
+            x3[:3], magnification_xy=mxy, magnification_z=mz, radius=r, sensitivity=s,
+            mode=mode, doIntensityWeighting=bool(iw), run_type="Threaded"))
+    # the workflow: timepoints of 2 frames (last one short), per-slice MPC
+    tps = []
+    for t0 in range(0, 5, 2):
+        v = R["eSRRF3D_ST"](verbose=False).run(x3[t0:t0 + 2], magnification_xy=2,
+                                                magnification_z=2, radius=1.5, sensitivity=1,
+                                                run_type="Threaded")
+        tps.append(np.asarray(R["macro_pixel_corrector"](np.asarray(v), magnification=2)))
+    g["esrrf3d/workflow"] = np.stack(tps)
 
     keep64 = ("esrrf_st/cases",)
     g = {k: (np.asarray(v, dtype=np.float32) if k not in keep64 and "/vals" not in k

@@ -188,3 +188,20 @@ def test_oracle_qnr_of_the_sweep(golden):
             rsp[si, ri] = S.error_map(np.mean(xq, 0), rgc.mean(0))["rsp"]
             frc[si, ri] = S.fire_number(rgc[1::2].mean(0), rgc[::2].mean(0))[0]
     assert np.abs(S.qnr(rsp, frc) - golden["score/sweep/qnr"]).max() <= 1e-5
+
+
+# --- eSRRF-3D -------------------------------------------------------------------
+ESRRF3D_CASES = [(2, 2, 1.5, 1, "average", 1), (3, 1, 1.0, 2, "std", 1), (2, 3, 2.0, 1, "average", 0),
+                 (1, 2, 1.5, 1, "average", 1)]
+
+
+@pytest.mark.parametrize("k", range(len(ESRRF3D_CASES)))
+def test_oracle_esrrf3d_st(golden, k):
+    mxy, mz, r, s, mode, iw = ESRRF3D_CASES[k]
+    got = O.esrrf3d_st(golden["esrrf3d/input"][:3], mxy, mz, r, 2.8, 4.0, s, mode, bool(iw))
+    assert rel_err(got, golden[f"esrrf3d/{k}"]) <= 1e-5
+
+
+def test_oracle_esrrf3d_workflow(golden):
+    got = O.esrrf3d(golden["esrrf3d/input"], 2, 2, 1.5, frames_per_timepoint=2)
+    assert rel_err(got, golden["esrrf3d/workflow"]) <= 1e-5

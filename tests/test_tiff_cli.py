@@ -1,0 +1,101 @@
+"""TIFF codec and command-line front door (no GPU: the reconstruction is
+replaced by a stand-in where a test needs one)."""
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+from nanopyx_gb300 import cli, tiff
+
+
+@pytest.mark.parametrize("shape,dtype", [((5, 7), np.float32), ((3, 6, 4), np.float32),
+                                         ((2, 3, 4, 5), np.float32), ((9, 8), np.uint16),
+                                         ((2, 5, 5), np.int32), ((4, 3), np.float64)])
+@pytest.mark.parametrize("big", [False, True])
+def test_round_trip(tmp_path, shape, dtype, big):
+    rng = np.random.default_rng(1)
+    a = (rng.random(shape) * 1000).astype(dtype)
+    p = tmp_path / "a.tif"
+    p.write_bytes(tiff._encode(a, bigtiff=big))
+    b = tiff._decode(p.read_bytes())
+    assert b.dtype == a.dtype and b.shape == a.shape and np.array_equal(a, b)
+
+
+def _classic_be(pages, compress=None, predictor=1):
+    """A big-endian uint16 TIFF of several pages, each in 2-row strips."""
+    out = bytearray(b"MM" + struct.pack(">HI", 42, 0))
+    prev = 4
+    for img in pages:
+        H, W = img.shape
+        offs, cnts = [], []
+        for r in range(0, H, 2):
+            rows = img[r:r + 2].astype(">u2")
+            if predictor == 2:
+                rows = np.concatenate([rows[:, :1], np.diff(rows, axis=1)], axis=1).astype(">u2")
+            raw = rows.tobytes()
+            if compress == "deflate":
+                raw = zlib.compress(raw)
+            offs.append(len(out))
+            cnts.append(len(raw))
+            out += raw
+            if len(out) % 2:
+                out += b"\0"
+        so = len(out)
+        out += struct.pack(">" + "I" * len(offs), *offs)
+        sc = len(out)
+        out += struct.pack(">" + "I" * len(cnts), *cnts)
+        ent = [(256, 3, 1, W), (257, 3, 1, H), (258, 3, 1, 16),
+               (259, 3, 1, 8 if compress == "deflate" else 1), (262, 3, 1, 1),
+               (273, 4, len(offs), so), (277, 3, 1, 1), (278, 3, 1, 2),
+               (279, 4, len(cnts), sc), (317, 3, 1, predictor)]
+        ifd = len(out)
+        out += struct.pack(">H", len(ent))
+        for tag, typ, cnt, val in ent:
+            out += struct.pack(">HHI", tag, typ, cnt)
+            out += struct.pack(">HH", val, 0) if typ == 3 and cnt == 1 else struct.pack(">I", val)
+        link = len(out)
+        out += struct.pack(">I", 0)
+        struct.pack_into(">I", out, prev, ifd)
+        prev = link
+    return bytes(out)
+
+
+@pytest.mark.parametrize("compress,predictor", [(None, 1), ("deflate", 1), ("deflate", 2)])
+def test_reads_big_endian_multipage_strips(compress, predictor):
+    rng = np.random.default_rng(2)
+    pages = [rng.integers(0, 60000, (5, 6)).astype(np.uint16) for _ in range(3)]
+    got = tiff._decode(_classic_be(pages, compress, predictor))
+    assert got.shape == (3, 5, 6) and got.dtype == np.uint16
+    assert np.array_equal(got, np.stack(pages))
+
+
+def test_rejects_non_tiff():
+    with pytest.raises(ValueError):
+        tiff._decode(b"PK\x03\x04")
+
+
+def test_cli_esrrf_maps_arguments_and_writes_tiff(tmp_path, monkeypatch):
+    from nanopyx_gb300 import methods
+
+    seen = {}
+
+    def fake_esrrf(image, **kw):
+        seen.update(kw, shape=image.shape)
+        return np.full((1, 4, 4), 7.0, np.float32)
+
+    monkeypatch.setattr(methods, "eSRRF", fake_esrrf)
+    src, dst = tmp_path / "in.tif", tmp_path / "out.tif"
+    tiff.imwrite(str(src), np.ones((6, 8, 8), np.float32))
+    assert cli.main(["linkinpy-SuperResolution-eSRRF", str(src), str(dst), "--magnification",
+                     "2", "--radius", "2.0", "--temporal-correlation", "VAR",
+                     "--no-macro-pixel-correction", "--pad-edges"]) == 0
+    assert seen["shape"] == (6, 8, 8) and seen["magnification"] == 2
+    assert seen["radius"] == 2.0 and seen["temporal_correlation"] == "VAR"
+    assert seen["macro_pixel_correction"] is False and seen["pad_edges"] is True
+    assert seen["use_fht"] is False and seen["doIntensityWeighting"] is True
+    assert np.array_equal(tiff.imread(str(dst)), np.full((1, 4, 4), 7.0, np.float32))
+
+
+def test_cli_unknown_command():
+    assert cli.main(["linkinpy-Restoration-NLMDenoising"]) == 2
