@@ -430,6 +430,8 @@ def run_gpu_arm(args):
         torch.cuda.empty_cache()
         line["sweep_scored"] = bench_scored_sweep(dev)
         torch.cuda.empty_cache()
+        line["esrrf3d"] = bench_esrrf3d(dev)
+        torch.cuda.empty_cache()
         # arrival-rate sweep of the served stream (rates bracket the device's
         # capacity for this request mix); "served" is the highest rate
         blocks = served_blocks([64, 90, 128, 181, 256, 362, 512, 724, 1024])
@@ -650,6 +652,44 @@ def bench_scored_sweep(dev, repeats=3):
                             "fire_gpu": float(frc[si, ri]), "fire_reference": float(fire_ref)}}
         out["speedup_vs_reference_extrapolated"] = est / t_sweep
     return out
+
+
+def bench_esrrf3d(dev, T=20, S=16, H=128, W=128, repeats=3):
+    """eSRRF-3D of a (20, 16, 128, 128) stack at magnification 2 x 2 (R = 1.5,
+    PSF ratio 2.8, voxel ratio 4, average), inputs resident on the device;
+    beside it the compiled reference's eSRRF3D_ST on 2 frames of the stack."""
+    import torch
+
+    import nanopyx_gb300 as nx
+
+    rng = np.random.default_rng(1)
+    x_np = (rng.random((T, S, H, W)) * 200 + 20).astype(np.float32)
+    x = torch.from_numpy(x_np).to(dev)
+    op = nx.eSRRF3D_ST(verbose=False)
+    op.run(x[:2])
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(repeats):
+        out = op.run(x)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) / repeats / 1e3
+    vox = int(out.numel()) * T
+    res = {"workload": f"eSRRF-3D {T}x{S}x{H}x{W}, m_xy=2, m_z=2, R=1.5, average",
+           "seconds": t, "value": vox / t / 1e6, "unit": "output Mvoxel*frames/s"}
+    if cpu_reference_available():
+        from oracle import ref_build
+
+        R = ref_build.load()
+        t0 = time.perf_counter()
+        R["eSRRF3D_ST"](verbose=False).run(x_np[:2], run_type="Threaded")
+        tr = (time.perf_counter() - t0) / 2
+        res["reference"] = {"kind": "reference", "cores": os.cpu_count(),
+                            "sample": "compiled reference eSRRF3D_ST(Threaded), 2 frames",
+                            "seconds_per_frame": tr, "value": vox / T / tr / 1e6}
+        res["speedup_vs_reference"] = tr * T / t
+    return res
 
 
 SERVED_RATES = (5.0, 10.0, 20.0, 30.0)

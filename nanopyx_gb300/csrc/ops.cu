@@ -77,8 +77,8 @@ __global__ void cr_shift_magnify_kernel(const float* __restrict__ in, int T, int
 // cr_shift_magnify_kernel, so the same results, with 4 shared loads and one
 // coalesced store per output instead of 16 global loads and 20 weight
 // evaluations.
-constexpr int kCrTileRows = 32;
 constexpr int kCrTileCols = 256;
+constexpr int kCrMaxTileRows = 128;
 
 // Patch rows / columns a tile can touch at magnification mag >= 1: the taps of
 // n consecutive outputs start within floor((n - 1) / mag) + 1 input pixels of
@@ -88,19 +88,33 @@ inline int cr_patch_extent(int n_out, float mag) {
   return (int)std::floor((double)(n_out - 1) / (double)mag) + 6;
 }
 
+// shared memory of a tile of `rows` output rows
+inline size_t cr_tile_smem(int rows, float mag_r, float mag_c) {
+  const int PR = cr_patch_extent(rows, mag_r), PC = cr_patch_extent(kCrTileCols, mag_c);
+  return (size_t)(PR + rows) * PC * sizeof(float) + rows * (sizeof(float4) + sizeof(int));
+}
+
+// Output rows per tile: the most (up to 128) whose staging fits in 72 KB, so
+// that the stores of a tile outweigh its weight set-up and patch load
+inline int cr_tile_rows(float mag_r, float mag_c) {
+  for (int rows = kCrMaxTileRows; rows > 32; rows /= 2)
+    if (cr_tile_smem(rows, mag_r, mag_c) <= 72 * 1024) return rows;
+  return 32;
+}
+
 __global__ void __launch_bounds__(kCrTileCols)
     cr_magnify_tiled_kernel(const float* __restrict__ in, int H, int W,
                             const float* __restrict__ shift_r, const float* __restrict__ shift_c,
-                            float mag_r, float mag_c, int rowsM, int colsM, int PR, int PC,
-                            float* __restrict__ out) {
+                            float mag_r, float mag_c, int rowsM, int colsM, int TR, int PR,
+                            int PC, float* __restrict__ out) {
   // the float4 row weights first, at the 16-byte aligned base
   extern __shared__ __align__(16) float crs[];
-  float4* wr = reinterpret_cast<float4*>(crs);                  // [kCrTileRows]
-  int* rbase = reinterpret_cast<int*>(wr + kCrTileRows);        // [kCrTileRows]
-  float* patch = reinterpret_cast<float*>(rbase + kCrTileRows); // [PR][PC]
-  float* P = patch + PR * PC;                                   // [kCrTileRows][PC]
+  float4* wr = reinterpret_cast<float4*>(crs);                  // [TR]
+  int* rbase = reinterpret_cast<int*>(wr + TR);                 // [TR]
+  float* patch = reinterpret_cast<float*>(rbase + TR);          // [PR][PC]
+  float* P = patch + PR * PC;                                   // [TR][PC]
   const int t = blockIdx.z;
-  const int i0 = blockIdx.y * kCrTileRows;
+  const int i0 = blockIdx.y * TR;
   const int j0 = blockIdx.x * kCrTileCols;
   const float sr = shift_r[t], sc = shift_c[t];
   const int tid = threadIdx.x;
@@ -118,8 +132,8 @@ __global__ void __launch_bounds__(kCrTileCols)
   float wc[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) wc[k] = cr_cubic(col - ((float)(c_int - 1 + k) + 0.5f));
-  if (tid < kCrTileRows) {
-    const int i = i0 + tid;
+  for (int il = tid; il < TR; il += kCrTileCols) {
+    const int i = i0 + il;
     const float row = __fsub_rn(__fdiv_rn((float)i, mag_r), sr);
     const int r_int = (int)floorf(row - 0.5f);
     const int rb = r_int - 1 - pr0;
@@ -127,8 +141,8 @@ __global__ void __launch_bounds__(kCrTileCols)
     float w[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) w[k] = cr_cubic(row - ((float)(r_int - 1 + k) + 0.5f));
-    wr[tid] = make_float4(w[0], w[1], w[2], w[3]);
-    rbase[tid] = rval ? rb : -1;
+    wr[il] = make_float4(w[0], w[1], w[2], w[3]);
+    rbase[il] = rval ? rb : -1;
   }
   const float* f = in + (size_t)t * H * W;
   for (int idx = tid; idx < PR * PC; idx += kCrTileCols) {
@@ -138,7 +152,7 @@ __global__ void __launch_bounds__(kCrTileCols)
   __syncthreads();
   // vertical pass: P[i][c] = sum_l w_l(i) patch[rbase(i) + l][c] (fma order of
   // the per-pixel kernel: l = 0..3)
-  for (int idx = tid; idx < kCrTileRows * PC; idx += kCrTileCols) {
+  for (int idx = tid; idx < TR * PC; idx += kCrTileCols) {
     const int il = idx / PC, c = idx % PC;
     const int rb = rbase[il];
     float p = 0.f;
@@ -155,7 +169,7 @@ __global__ void __launch_bounds__(kCrTileCols)
   __syncthreads();
   if (j >= colsM) return;
   float* o = out + (size_t)t * rowsM * colsM + j;
-  const int iend = min(kCrTileRows, rowsM - i0);
+  const int iend = min(TR, rowsM - i0);
   for (int il = 0; il < iend; ++il) {
     float q = 0.f;
     if (cval && rbase[il] >= 0) {
@@ -689,13 +703,11 @@ cudaError_t launch_cr_shift_magnify(const float* in, int T, int H, int W, const 
                                     int colsM, float* out, cudaStream_t s) {
   const long long n = (long long)T * rowsM * colsM;
   if (n == 0) return cudaSuccess;
-  if (mag_r >= 1.f && mag_c >= 1.f && T <= 65535 && rowsM / kCrTileRows < 65535) {
-    // shared memory for the largest patch (magnification 1); each launch uses
-    // the extent its magnifications need
-    static const size_t smem_max =
-        (size_t)(cr_patch_extent(kCrTileRows, 1.f) + kCrTileRows) *
-            cr_patch_extent(kCrTileCols, 1.f) * sizeof(float) +
-        kCrTileRows * (sizeof(float4) + sizeof(int));
+  if (mag_r >= 1.f && mag_c >= 1.f && T <= 65535 && rowsM / 32 < 65535) {
+    // shared memory for the largest tile staging (32 rows at magnification 1,
+    // or any tile cr_tile_rows picks: <= 72 KB); each launch uses what its
+    // magnifications need
+    static const size_t smem_max = std::max<size_t>(cr_tile_smem(32, 1.f, 1.f), 72 * 1024);
     static int attr_dev = -1;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -706,13 +718,13 @@ cudaError_t launch_cr_shift_magnify(const float* in, int T, int H, int W, const 
       if (e != cudaSuccess) return e;
       attr_dev = dev;
     }
-    const int PR = cr_patch_extent(kCrTileRows, mag_r), PC = cr_patch_extent(kCrTileCols, mag_c);
-    const size_t smem = (size_t)(PR + kCrTileRows) * PC * sizeof(float) +
-                        kCrTileRows * (sizeof(float4) + sizeof(int));
+    const int TR = cr_tile_rows(mag_r, mag_c);
+    const int PR = cr_patch_extent(TR, mag_r), PC = cr_patch_extent(kCrTileCols, mag_c);
+    const size_t smem = cr_tile_smem(TR, mag_r, mag_c);
     const dim3 grid((unsigned)((colsM + kCrTileCols - 1) / kCrTileCols),
-                    (unsigned)((rowsM + kCrTileRows - 1) / kCrTileRows), (unsigned)T);
+                    (unsigned)((rowsM + TR - 1) / TR), (unsigned)T);
     cr_magnify_tiled_kernel<<<grid, kCrTileCols, smem, s>>>(in, H, W, shift_r, shift_c, mag_r,
-                                                            mag_c, rowsM, colsM, PR, PC, out);
+                                                            mag_c, rowsM, colsM, TR, PR, PC, out);
     return cudaGetLastError();
   }
   cr_shift_magnify_kernel<<<grid_for(n), kBlock, 0, s>>>(in, T, H, W, shift_r, shift_c, mag_r,
