@@ -573,7 +573,7 @@ def bench_sweep(dev, repeats=3):
                                 for (m, J), v in sorted(grid.batch.tiling.items())}}}
 
 
-def bench_scored_sweep(dev, repeats=3):
+def bench_scored_sweep(dev, repeats=3, with_reference=True):
     """The scored sweep of the same grid: ParameterSweep.run -- reconstructions
     over all, odd and even frames, ErrorMap RSP of all 16 pairs (one lockstep
     Brent search), FRC of all 16 pairs (one batch of FFTs), QnR.
@@ -616,7 +616,7 @@ def bench_scored_sweep(dev, repeats=3):
            "seconds": t_sweep, "reconstructions_s": t1 - t0, "error_maps_s": t2 - t1,
            "frc_s": t3 - t2, "brent_evaluations": int(sum(em["evaluations"])),
            "qnr_best": [sens[int(np.argmax(q)) // 4], radii[int(np.argmax(q)) % 4]]}
-    if cpu_reference_available():
+    if with_reference and cpu_reference_available():
         from oracle import ref_build
 
         R = ref_build.load()
@@ -654,7 +654,7 @@ def bench_scored_sweep(dev, repeats=3):
     return out
 
 
-def bench_esrrf3d(dev, T=20, S=16, H=128, W=128, repeats=3):
+def bench_esrrf3d(dev, T=20, S=16, H=128, W=128, repeats=3, with_reference=True):
     """eSRRF-3D of a (20, 16, 128, 128) stack at magnification 2 x 2 (R = 1.5,
     PSF ratio 2.8, voxel ratio 4, average), inputs resident on the device;
     beside it the compiled reference's eSRRF3D_ST on 2 frames of the stack."""
@@ -678,7 +678,7 @@ def bench_esrrf3d(dev, T=20, S=16, H=128, W=128, repeats=3):
     vox = int(out.numel()) * T
     res = {"workload": f"eSRRF-3D {T}x{S}x{H}x{W}, m_xy=2, m_z=2, R=1.5, average",
            "seconds": t, "value": vox / t / 1e6, "unit": "output Mvoxel*frames/s"}
-    if cpu_reference_available():
+    if with_reference and cpu_reference_available():
         from oracle import ref_build
 
         R = ref_build.load()
@@ -936,6 +936,7 @@ def main():
                     help="frames of the standalone-op measurement")
     ap.add_argument("--scored-sweep-only", action="store_true",
                     help="only the scored parameter sweep (RSP / FRC / QnR)")
+    ap.add_argument("--esrrf3d-only", action="store_true", help="only the eSRRF-3D measurement")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the uneven-batch, sweep and served-stream measurements")
     ap.add_argument("--served-requests", type=int, default=200,
@@ -956,11 +957,13 @@ def main():
         print(json.dumps(bench_standalone_ops(torch.device("cuda", 0), T=args.ops_frames)),
               flush=True)
         return 0
-    if args.scored_sweep_only:
+    if args.scored_sweep_only or args.esrrf3d_only:
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps(bench_scored_sweep(torch.device("cuda", 0))), flush=True)
+        dev = torch.device("cuda", 0)
+        fn = bench_scored_sweep if args.scored_sweep_only else bench_esrrf3d
+        print(json.dumps(fn(dev, with_reference=not args.no_cpu_baseline)), flush=True)
         return 0
     if args.srrf_only:
         import torch
