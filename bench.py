@@ -611,11 +611,19 @@ def bench_scored_sweep(dev, repeats=3, with_reference=True):
     t2 = time.perf_counter()
     frc = ps._fire_grid(rec[1], rec[2])
     t3 = time.perf_counter()
+    img = rec[0][1, 1, 0].contiguous()  # s = 2, R = 1.5
+    nx.DecorrAnalysis().run_analysis(img)
+    torch.cuda.synchronize(dev)
+    t4 = time.perf_counter()
+    dec_gpu = nx.DecorrAnalysis().run_analysis(img)
+    torch.cuda.synchronize(dev)
+    t_dec = time.perf_counter() - t4
     out = {"workload": "scored sweep: 200x256x256, m=4, R in {1,1.5,2,2.5} x s in {1,2,3,4}, "
                        "AVG; reconstructions (all/odd/even frames), RSP, FRC, QnR",
            "seconds": t_sweep, "reconstructions_s": t1 - t0, "error_maps_s": t2 - t1,
            "frc_s": t3 - t2, "brent_evaluations": int(sum(em["evaluations"])),
-           "qnr_best": [sens[int(np.argmax(q)) // 4], radii[int(np.argmax(q)) % 4]]}
+           "qnr_best": [sens[int(np.argmax(q)) // 4], radii[int(np.argmax(q)) % 4]],
+           "decorrelation_1024x1024_s": t_dec}
     if with_reference and cpu_reference_available():
         from oracle import ref_build
 
@@ -636,6 +644,10 @@ def bench_scored_sweep(dev, repeats=3, with_reference=True):
                                                                rec[2][si, ri, 0].cpu().numpy())
         t2 = time.perf_counter()
         t_score = t2 - t0
+        dcr = R["DecorrAnalysis"]()
+        t3 = time.perf_counter()
+        dcr.run_analysis(img.cpu().numpy())
+        t_dec_ref = time.perf_counter() - t3
         est = 16 * (200 * t_frame + t_score)
         out["reference"] = {
             "kind": "reference", "cores": os.cpu_count(),
@@ -649,7 +661,10 @@ def bench_scored_sweep(dev, repeats=3, with_reference=True):
             "pair_parity": {"sigma_gpu": em["sigma"][si * 4 + ri],
                             "sigma_reference": emr.get_sigma(),
                             "rsp_gpu": em["rsp"][si * 4 + ri], "rsp_reference": emr.getRSP(),
-                            "fire_gpu": float(frc[si, ri]), "fire_reference": float(fire_ref)}}
+                            "fire_gpu": float(frc[si, ri]), "fire_reference": float(fire_ref),
+                            "decorrelation_gpu": dec_gpu,
+                            "decorrelation_reference": float(dcr.resolution)},
+            "decorrelation_s": t_dec_ref}
         out["speedup_vs_reference_extrapolated"] = est / t_sweep
     return out
 

@@ -312,6 +312,14 @@ size_t nx_gaussian_blur_batch_workspace_bytes(int H, int W, int n);
 int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
                            const double* sigma, const float* alpha, const float* beta,
                            float* d_out, void* d_ws, size_t ws_bytes, void* stream);
+/* flags: NX_BLUR_FLOAT64_SUMS accumulates every pass in float64 and rounds it
+ * to float32 (scipy's own arithmetic for float32 arrays: exact for the
+ * near-identity blurs whose difference from the image is the signal).       */
+#define NX_BLUR_FLOAT64_SUMS 1
+int nx_gaussian_blur_batch_ex(const float* d_in, int H, int W, int n, const int* src_index,
+                              const double* sigma, const float* alpha, const float* beta,
+                              int flags, float* d_out, void* d_ws, size_t ws_bytes,
+                              void* stream);
 
 /* Float64 moment sums of `batch` images d_x (batch, n) against one image
  * d_y (n): per image sum x, sum y, sum x^2, sum x y, sum y^2 and
@@ -338,6 +346,27 @@ size_t nx_frc_workspace_bytes(const nx_frc_plan* plan, int pairs);
 int nx_frc_ring_sums(const nx_frc_plan* plan, const float* d_img1, const float* d_img2, int pairs,
                      long long stride, int pitch, int r0, int c0, double* d_sums, void* d_ws,
                      size_t ws_bytes, void* stream);
+
+/* Decorrelation analysis (src/nanopyx/core/analysis/decorr.pyx:23-393).
+ * nx_decorr_prepare: the (h, w) image with its 20-pixel border rolled off
+ * towards the mean outside the circle of radius w/2 - 20
+ * (src/nanopyx/core/transform/edges.pyx:9-49), placed in the N x N square
+ * (N the power of two >= max(h, w)) at rows 0 .. h-1 and columns (N-w)/2 ..,
+ * the rest filled with its first pixel (decorr.pyx:64-99).
+ * nx_decorr_coefs: for B N x N images -- d_base[z], or d_base - d_sub[z]
+ * (the high-pass differences) when d_sub is given -- the centred spectrum
+ * (DC term zeroed when zero_dc), d_cr[z] = sum over the inscribed disc of
+ * |F|^2, and d_coef[z] (2 n_r doubles): per radial bin of the band
+ * [crmin, crmax] the sum of re^2/|F| + im^2/|F| and of the normalised power,
+ * over the reference's walk of the centred square (decorr.pyx:120-200).
+ * Uses an nx_frc_plan of size N for the transforms.                        */
+size_t nx_decorr_prepare_workspace_bytes(int h, int w);
+int nx_decorr_prepare(const float* d_img, int h, int w, float* d_out, int N, void* d_ws,
+                      size_t ws_bytes, void* stream);
+size_t nx_decorr_coefs_workspace_bytes(const nx_frc_plan* plan, int B, int n_r);
+int nx_decorr_coefs(const nx_frc_plan* plan, const float* d_base, const float* d_sub, int B,
+                    int zero_dc, float crmin, float crmax, int n_r, double* d_cr,
+                    double* d_coef, void* d_ws, size_t ws_bytes, void* stream);
 
 /* Macro-pixel correction in place on (S, rowsM, colsM).
  *   src/nanopyx/core/transform/mpcorrector.pyx:7-73                         */

@@ -8,7 +8,8 @@ from ._native import DeviceTimeoutError, NativeLibraryError
 from .liquid import LiquidEngine
 from .methods import (SRRF, ESRRFAccumulator, Workflow, eSRRF, eSRRF3D, esrrf_device,
                       esrrf_parameter_sweep)
-from .scoring import (ErrorMap, FIRECalculator, ParameterSweep, calculate_error_map, calculate_frc,
+from .scoring import (DecorrAnalysis, ErrorMap, FIRECalculator, ParameterSweep,
+                      calculate_decorr_analysis, calculate_error_map, calculate_frc,
                       run_esrrf_parameter_sweep)
 from .transform import (CRShiftAndMagnify, GradientRobertsCross, RadialGradientConvergence,
                         Radiality, ShiftAndMagnify, calculate_eSRRF_temporal_correlations,
@@ -25,5 +26,5 @@ __all__ = [
     "calculate_SRRF_temporal_correlations", "macro_pixel_corrector", "check_image",
     "value2array", "fht_space_interpolation", "LiquidEngine", "NativeLibraryError",
     "DeviceTimeoutError", "ErrorMap", "FIRECalculator", "ParameterSweep", "calculate_error_map",
-    "calculate_frc",
+    "calculate_frc", "DecorrAnalysis", "calculate_decorr_analysis",
 ]

@@ -105,6 +105,11 @@ _SIGS = {
     "nx_gaussian_blur": (_I, [_P, _I, _I, C.c_double, _I, C.c_float, C.c_float, _P, _P, _SZ, _P]),
     "nx_gaussian_blur_batch_workspace_bytes": (_SZ, [_I, _I, _I]),
     "nx_gaussian_blur_batch": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "nx_gaussian_blur_batch_ex": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _I, _P, _P, _SZ, _P]),
+    "nx_decorr_prepare_workspace_bytes": (_SZ, [_I, _I]),
+    "nx_decorr_prepare": (_I, [_P, _I, _I, _P, _I, _P, _SZ, _P]),
+    "nx_decorr_coefs_workspace_bytes": (_SZ, [_P, _I, _I]),
+    "nx_decorr_coefs": (_I, [_P, _P, _P, _I, _I, C.c_float, C.c_float, _I, _P, _P, _P, _SZ, _P]),
     "nx_moment_sums_workspace_bytes": (_SZ, [_I]),
     "nx_moment_sums": (_I, [_P, _P, C.c_longlong, _I, _P, _P, _SZ, _P]),
     "nx_frc_plan_create": (_I, [C.POINTER(_P), _I]),

@@ -1,13 +1,14 @@
 """Command-line front door: TIFF in, reconstruction or metric out.
 
 The reference's console scripts (src/nanopyx/cli/superresolution.py:10-192,
-src/nanopyx/cli/metrics.py:18-96; pyproject.toml:64-74), with the same
+src/nanopyx/cli/metrics.py:18-145; pyproject.toml:64-74), with the same
 functions, arguments, defaults and outputs, computing on the GPU:
 
     python -m nanopyx_gb300.cli linkinpy-SuperResolution-eSRRF in.tif out.tif --radius 1.5
     python -m nanopyx_gb300.cli linkinpy-SuperResolution-SRRF in.tif out.tif
     python -m nanopyx_gb300.cli linkinpy-Metrics-CalculateErrorMap ref.tif sr.tif map.tif
     python -m nanopyx_gb300.cli linkinpy-Metrics-CalculateFRC a.tif b.tif frc.csv
+    python -m nanopyx_gb300.cli linkinpy-Metrics-ImageDecorrelationAnalysis sr.tif dec.csv
 """
 from __future__ import annotations
 
@@ -160,11 +161,47 @@ def linkinpy_calculate_frc_main(argv=None) -> None:
                            a.units, a.plot_frc_curve)
 
 
+def linkinpy_calculate_decorr_analysis(input_image: str, output_csv: str, rmin: float = 0.0,
+                                       rmax: float = 1.0, n_r: int = 50, n_g: int = 10,
+                                       pixel_size: float = 1.0, units: str = "pixel",
+                                       roi: str = "0,0,0,0",
+                                       plot_decorr_analysis: bool = False) -> None:
+    from .scoring import calculate_decorr_analysis
+
+    roi_tuple = tuple(int(v.strip()) for v in roi.split(","))
+    resolution = calculate_decorr_analysis(frame=imread(input_image), rmin=rmin, rmax=rmax,
+                                           n_r=n_r, n_g=n_g, pixel_size=pixel_size,
+                                           units=units, roi=roi_tuple,
+                                           plot_decorr_analysis=plot_decorr_analysis)
+    _write_scalar_csv(output_csv, "decorr_resolution", float(resolution))
+
+
+def linkinpy_calculate_decorr_analysis_main(argv=None) -> None:
+    parser = argparse.ArgumentParser(description="Calculate decorrelation-based resolution.")
+    parser.add_argument("input_image", help="Input image path.")
+    parser.add_argument("output_csv", help="Output CSV path.")
+    parser.add_argument("--rmin", type=float, default=0.0)
+    parser.add_argument("--rmax", type=float, default=1.0)
+    parser.add_argument("--n-r", "--n_r", dest="n_r", type=int, default=50)
+    parser.add_argument("--n-g", "--n_g", dest="n_g", type=int, default=10)
+    parser.add_argument("--pixel-size", "--pixel_size", dest="pixel_size", type=float,
+                        default=1.0)
+    parser.add_argument("--units", default="pixel")
+    parser.add_argument("--roi", default="0,0,0,0")
+    _bool(parser, "--plot-decorr-analysis", "--plot_decorr_analysis",
+          dest="plot_decorr_analysis", default=False)
+    a = parser.parse_args(argv)
+    linkinpy_calculate_decorr_analysis(a.input_image, a.output_csv, a.rmin, a.rmax, a.n_r,
+                                       a.n_g, a.pixel_size, a.units, a.roi,
+                                       a.plot_decorr_analysis)
+
+
 COMMANDS = {
     "linkinpy-SuperResolution-SRRF": linkinpy_SRRF_main,
     "linkinpy-SuperResolution-eSRRF": linkinpy_eSRRF_main,
     "linkinpy-Metrics-CalculateErrorMap": linkinpy_calculate_error_map_main,
     "linkinpy-Metrics-CalculateFRC": linkinpy_calculate_frc_main,
+    "linkinpy-Metrics-ImageDecorrelationAnalysis": linkinpy_calculate_decorr_analysis_main,
 }
 
 

@@ -67,18 +67,20 @@ struct BlurBatch {
 };
 
 // scipy's weights of one image and axis (blockIdx.x, blockIdx.y), in float64,
-// normalised, folded onto the reflection period when the kernel is longer
+// normalised, folded onto the reflection period when the kernel is longer;
+// stored as A (float, or double for float64 accumulation)
+template <typename A>
 __global__ void gauss_weights_kernel(const __grid_constant__ BlurBatch b, int H, int W,
-                                     float* __restrict__ w0, float* __restrict__ w1) {
+                                     A* __restrict__ w0, A* __restrict__ w1) {
   __shared__ double red[256];
   const int z = blockIdx.x, axis = blockIdx.y;
   const int n = axis ? W : H;
-  float* w = axis ? w1 + (size_t)z * 2 * W : w0 + (size_t)z * 2 * H;
+  A* w = axis ? w1 + (size_t)z * 2 * W : w0 + (size_t)z * 2 * H;
   const BlurAxis ax = b.ax[axis][z];
   const double sigma = b.sigma[z];
   const int radius = b.radius[z];
   if (!(sigma > 1e-15)) {
-    if (threadIdx.x == 0) w[0] = 1.f;
+    if (threadIdx.x == 0) w[0] = (A)1;
     return;
   }
   const double c = -0.5 / (sigma * sigma);
@@ -97,7 +99,7 @@ __global__ void gauss_weights_kernel(const __grid_constant__ BlurBatch b, int H,
   if (!ax.fold) {
     for (int k = threadIdx.x; k <= 2 * radius; k += blockDim.x) {
       const double x = (double)(k - radius);
-      w[k] = (float)(exp(c * x * x) / total);
+      w[k] = (A)(exp(c * x * x) / total);
     }
     return;
   }
@@ -107,56 +109,74 @@ __global__ void gauss_weights_kernel(const __grid_constant__ BlurBatch b, int H,
     double acc = 0.0;
     const long long d0 = j - (long long)((j + radius) / p) * p;  // smallest d >= -radius
     for (long long d = d0; d <= radius; d += p) acc += exp(c * (double)d * (double)d) / total;
-    w[j] = (float)acc;
+    w[j] = (A)acc;
   }
+}
+
+template <typename A>
+__device__ __forceinline__ A mac(A w, float v, A acc) {
+  return fma(w, (A)v, acc);
 }
 
 // axis 0: out[z][y][x] = sum_j w[j] * src[reflect(y + offset + j)][x], the
 // source mapped to alpha * v + beta first when the batch is affine.  A CTA
 // computes 32 columns x 64 rows (8 rows per thread); with up to kStageTaps
 // taps the weights and the column strip with its reflected halo rows are
-// staged in shared memory, else the taps are read through the cache.
+// staged in shared memory, else the taps are read through the cache.  The
+// accumulator is A; each pass rounds to float32 (as scipy writes a float32
+// output array axis by axis).
 constexpr int kTileCols = 32, kTileRows = 64, kRowsPerThread = 8;
 constexpr int kStageTaps = 256;
+template <typename A>
 __global__ void __launch_bounds__(256) blur_axis0_kernel(const __grid_constant__ BlurBatch b,
                                                          const float* __restrict__ in, int H,
-                                                         int W, const float* __restrict__ w0,
+                                                         int W, const A* __restrict__ w0,
                                                          int staged, float* __restrict__ mid) {
-  extern __shared__ float sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   const int z = blockIdx.z;
   const int x0 = blockIdx.x * kTileCols, y0 = blockIdx.y * kTileRows;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileCols + tx;
   const float* src = in + (size_t)b.src[z] * H * W;
-  const float* w = w0 + (size_t)z * 2 * H;
+  const A* w = w0 + (size_t)z * 2 * H;
   const BlurAxis ax = b.ax[0][z];
   const float alpha = b.alpha[z], beta = b.beta[z];
   const int x = x0 + tx;
-  float acc[kRowsPerThread];
+  A acc[kRowsPerThread];
 #pragma unroll
-  for (int q = 0; q < kRowsPerThread; ++q) acc[q] = 0.f;
+  for (int q = 0; q < kRowsPerThread; ++q) acc[q] = (A)0;
   if (staged) {
-    float* ws = sm;
-    float* tile = sm + kStageTaps;
+    A* ws = reinterpret_cast<A*>(smraw);
+    float* tile = reinterpret_cast<float*>(ws + kStageTaps);
     for (int k = tid; k < ax.taps; k += 256) ws[k] = w[k];
+    // rows of the strip, 8 in flight per thread (the row index, reflected,
+    // is the same for a whole warp: kTileCols = 32 lanes = one row)
     const int rows = kTileRows + ax.taps - 1;
-    for (int idx = tid; idx < rows * kTileCols; idx += 256) {
-      const int k = idx / kTileCols, c = idx % kTileCols;
-      int r = y0 + ax.offset + k;
-      if (r < 0 || r >= H) r = (int)reflect_index(r, H);
-      float v = 0.f;
-      if (x0 + c < W) {
-        v = __ldg(src + (size_t)r * W + x0 + c);
-        if (b.affine) v = __fadd_rn(__fmul_rn(alpha, v), beta);
+    const bool colok = x < W;
+    for (int k0 = ty; k0 < rows; k0 += 8 * 8) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u * 8;
+        v[u] = 0.f;
+        if (k < rows && colok) {
+          int r = y0 + ax.offset + k;
+          if (r < 0 || r >= H) r = (int)reflect_index(r, H);
+          v[u] = __ldg(src + (size_t)r * W + x);
+        }
       }
-      tile[idx] = v;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u * 8;
+        if (k < rows)
+          tile[k * kTileCols + tx] = b.affine ? __fadd_rn(__fmul_rn(alpha, v[u]), beta) : v[u];
+      }
     }
     __syncthreads();
     const float* col = tile + ty * kRowsPerThread * kTileCols + tx;
     for (int j = 0; j < ax.taps; ++j) {
-      const float wj = ws[j];
+      const A wj = ws[j];
 #pragma unroll
-      for (int q = 0; q < kRowsPerThread; ++q)
-        acc[q] = fmaf(wj, col[(q + j) * kTileCols], acc[q]);
+      for (int q = 0; q < kRowsPerThread; ++q) acc[q] = mac(wj, col[(q + j) * kTileCols], acc[q]);
     }
   } else if (x < W) {
 #pragma unroll
@@ -168,7 +188,7 @@ __global__ void __launch_bounds__(256) blur_axis0_kernel(const __grid_constant__
         if (r < 0 || r >= H) r = reflect_index(r, H);
         float v = __ldg(src + (size_t)r * W + x);
         if (b.affine) v = __fadd_rn(__fmul_rn(alpha, v), beta);
-        acc[q] = fmaf(__ldg(w + j), v, acc[q]);
+        acc[q] = mac(w[j], v, acc[q]);
       }
     }
   }
@@ -176,7 +196,7 @@ __global__ void __launch_bounds__(256) blur_axis0_kernel(const __grid_constant__
 #pragma unroll
     for (int q = 0; q < kRowsPerThread; ++q) {
       const int y = y0 + ty * kRowsPerThread + q;
-      if (y < H) mid[((size_t)z * H + y) * W + x] = acc[q];
+      if (y < H) mid[((size_t)z * H + y) * W + x] = (float)acc[q];
     }
   }
 }
@@ -184,18 +204,19 @@ __global__ void __launch_bounds__(256) blur_axis0_kernel(const __grid_constant__
 // axis 1: the row segment with its reflected halo (and the weights) staged in
 // shared memory when they fit, else read through the cache
 constexpr int kRowTile = 256;
+template <typename A>
 __global__ void __launch_bounds__(256) blur_axis1_kernel(const __grid_constant__ BlurBatch b,
                                                          const float* __restrict__ mid, int H,
-                                                         int W, const float* __restrict__ w1,
+                                                         int W, const A* __restrict__ w1,
                                                          int staged, float* __restrict__ out) {
-  extern __shared__ float sm[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   const int y = blockIdx.y, z = blockIdx.z;
   const int x0 = blockIdx.x * kRowTile;
   const float* row = mid + ((size_t)z * H + y) * W;
-  const float* w = w1 + (size_t)z * 2 * W;
+  const A* w = w1 + (size_t)z * 2 * W;
   const BlurAxis ax = b.ax[1][z];
-  float* ws = sm;
-  float* seg = sm + ((ax.taps + 3) & ~3);
+  A* ws = reinterpret_cast<A*>(smraw);
+  float* seg = reinterpret_cast<float*>(ws + ((ax.taps + 3) & ~3));
   if (staged) {
     for (int k = threadIdx.x; k < ax.taps; k += blockDim.x) ws[k] = w[k];
     const int span = kRowTile + ax.taps - 1;
@@ -209,19 +230,24 @@ __global__ void __launch_bounds__(256) blur_axis1_kernel(const __grid_constant__
   for (int t = threadIdx.x; t < kRowTile; t += blockDim.x) {
     const int x = x0 + t;
     if (x >= W) break;
-    float acc = 0.f;
+    A acc = (A)0;
     if (staged) {
-      for (int j = 0; j < ax.taps; ++j) acc = fmaf(ws[j], seg[t + j], acc);
+      for (int j = 0; j < ax.taps; ++j) acc = mac(ws[j], seg[t + j], acc);
     } else {
       for (int j = 0; j < ax.taps; ++j) {
         long long c = (long long)x + ax.offset + j;
         if (c < 0 || c >= W) c = reflect_index(c, W);
-        acc = fmaf(__ldg(w + j), __ldg(row + c), acc);
+        acc = mac(w[j], __ldg(row + c), acc);
       }
     }
-    out[((size_t)z * H + y) * W + x] = acc;
+    out[((size_t)z * H + y) * W + x] = (float)acc;
   }
 }
+
+template <typename A>
+int run_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
+                   const double* sigma, const float* alpha, const float* beta, float* d_out,
+                   char* base, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Moment sums of (x, y) pairs: sums and centred second moments in float64.
@@ -230,7 +256,7 @@ __global__ void __launch_bounds__(256) blur_axis1_kernel(const __grid_constant__
 // float64; the second moments are taken about the float32-rounded means
 // (two passes) and corrected to the exact means, so nothing cancels.
 // ---------------------------------------------------------------------------
-constexpr int kSumRun = 8;          // elements per thread and pass (short float32 runs)
+constexpr int kSumRun = 32;         // elements per thread and pass (short float32 runs)
 constexpr int kSumMaxBlocks = 2048;
 
 __device__ inline void block_sum(double* v, int nf, double* red /* [nf][blockDim] */) {
@@ -275,10 +301,12 @@ __global__ void __launch_bounds__(256) moment_mean_kernel(const float* __restric
   }
 }
 
-// per image: the two sums in fixed order
+// per image: the two sums in fixed order, and the means rounded to float
+// (sums: batch x 2 doubles; fmeans: batch x 2 floats)
 __global__ void __launch_bounds__(256) moment_mean_final_kernel(const double* __restrict__ part,
-                                                                int nparts,
-                                                                double* __restrict__ sums) {
+                                                                int nparts, long long n,
+                                                                double* __restrict__ sums,
+                                                                float* __restrict__ fmeans) {
   __shared__ double red[2 * 256];
   double v[2] = {0, 0};
   for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
@@ -289,6 +317,8 @@ __global__ void __launch_bounds__(256) moment_mean_final_kernel(const double* __
   if (threadIdx.x == 0) {
     sums[blockIdx.x * 2 + 0] = v[0];
     sums[blockIdx.x * 2 + 1] = v[1];
+    fmeans[blockIdx.x * 2 + 0] = (float)(v[0] / (double)n);
+    fmeans[blockIdx.x * 2 + 1] = (float)(v[1] / (double)n);
   }
 }
 
@@ -296,12 +326,12 @@ __global__ void __launch_bounds__(256) moment_mean_final_kernel(const double* __
 __global__ void __launch_bounds__(256) moment_centred_kernel(const float* __restrict__ x,
                                                              const float* __restrict__ y,
                                                              long long n,
-                                                             const double* __restrict__ sums,
+                                                             const float* __restrict__ fmeans,
                                                              double* __restrict__ part) {
   __shared__ double red[4 * 256];
   const int z = blockIdx.y;
   const float* xs = x + (size_t)z * n;
-  const float mx = (float)(sums[2 * z] / (double)n), my = (float)(sums[2 * z + 1] / (double)n);
+  const float mx = fmeans[2 * z], my = fmeans[2 * z + 1];
   double v[4] = {0, 0, 0, 0};
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n;
@@ -392,8 +422,8 @@ __device__ inline float2 csub(float2 a, float2 b) {
 __global__ void __launch_bounds__(kFftThreads) fft_lines_kernel(
     const __grid_constant__ FftPlanDev plan, const float2* __restrict__ tw, int mode,
     const float* __restrict__ rsrc0, const float* __restrict__ rsrc1, long long stride, int pitch,
-    int r0, int c0, const float* __restrict__ taper, const float2* __restrict__ csrc,
-    float2* __restrict__ dst) {
+    int r0, int c0, const float* __restrict__ taper, const float* __restrict__ sub,
+    const float2* __restrict__ csrc, float2* __restrict__ dst) {
   extern __shared__ float2 buf[];
   const int N = plan.N;
   const int line = blockIdx.x, z = blockIdx.y;
@@ -402,9 +432,17 @@ __global__ void __launch_bounds__(kFftThreads) fft_lines_kernel(
   if (mode == 0) {
     const float* row = ((z & 1) ? rsrc1 : rsrc0) + (size_t)(z >> 1) * stride +
                        (size_t)(r0 + line) * pitch + c0;
-    const float ty = taper[line];
-    for (int i = threadIdx.x; i < N; i += blockDim.x)
-      a[i] = make_float2(__fmul_rn(__fmul_rn(row[i], taper[i]), ty), 0.f);
+    if (taper) {
+      const float ty = taper[line];
+      for (int i = threadIdx.x; i < N; i += blockDim.x)
+        a[i] = make_float2(__fmul_rn(__fmul_rn(row[i], taper[i]), ty), 0.f);
+    } else if (sub) {  // high-pass line: base - sub_z (one N x N image each)
+      const float* srow = sub + ((size_t)z * N + line) * N;
+      for (int i = threadIdx.x; i < N; i += blockDim.x)
+        a[i] = make_float2(__fsub_rn(row[i], srow[i]), 0.f);
+    } else {
+      for (int i = threadIdx.x; i < N; i += blockDim.x) a[i] = make_float2(row[i], 0.f);
+    }
   } else {
     const float2* row = csrc + ((size_t)z * N + line) * N;
     for (int i = threadIdx.x; i < N; i += blockDim.x) a[i] = row[i];
@@ -509,10 +547,252 @@ __global__ void __launch_bounds__(256) frc_ring_kernel(const float2* __restrict_
 }
 
 
+// ---------------------------------------------------------------------------
+// Decorrelation analysis (src/nanopyx/core/analysis/decorr.pyx:64-118,
+// 120-214 with transform/edges.pyx:9-49): edge apodisation, the padded
+// square, the inscribed-disc spectral norm and the ring coefficients.
+// ---------------------------------------------------------------------------
+constexpr int kApodOffset = 20;  // pixels of the cosine roll-off
+
+// sum and count of the pixels outside the circle of radius w/2 - 20
+__global__ void __launch_bounds__(256) decorr_edge_kernel(const float* __restrict__ img, int h,
+                                                          int w, double* __restrict__ part) {
+  __shared__ double red[2 * 256];
+  const float radius = (float)(w / 2 - kApodOffset);
+  double v[2] = {0, 0};
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)h * w;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(e / w), x = (int)(e % w);
+    const int dy = y - h / 2, dx = x - w / 2;
+    const float dist = (float)(dy * dy + dx * dx);
+    if (dist > radius * radius) {
+      v[0] += img[e];
+      v[1] += 1.0;
+    }
+  }
+  block_sum(v, 2, red);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = v[0];
+    part[2 * blockIdx.x + 1] = v[1];
+  }
+}
+
+__device__ __forceinline__ float decorr_apodized(const float* img, int h, int w, int y, int x,
+                                                 float em) {
+  const float pin = img[(size_t)y * w + x];
+  const float x0 = fabsf((float)(x - w / 2)), y0 = fabsf((float)(y - h / 2));
+  const double ex = fabs((double)x0 - (double)(w / 2)), ey = fabs((double)y0 - (double)(h / 2));
+  if (ex <= kApodOffset || ey <= kApodOffset) {
+    const float d = (float)fmin(ex, ey);
+    const double pi = 3.14159265358979323846;
+    const float c = (float)((cos((double)d * pi / kApodOffset - pi) + 1) / 2);
+    return __fadd_rn(__fmul_rn(c, __fsub_rn(pin, em)), em);
+  }
+  if (abs(x - w / 2) > w / 2 && abs(y - h / 2) > h / 2) return em;
+  return pin;
+}
+
+// the N x N square: the apodised image at rows 0 .. h-1, columns ox .. ox+w-1
+// (ox = (N - w) / 2; the reference's copy loop leaves the row offset at 0),
+// every other pixel the apodised image's first pixel
+// the edge mean (float, as the reference keeps it) from the per-block sums
+__global__ void __launch_bounds__(256) decorr_edge_final_kernel(const double* __restrict__ part,
+                                                                int nparts,
+                                                                float* __restrict__ em) {
+  __shared__ double red[2 * 256];
+  double v[2] = {0, 0};
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
+    v[0] += part[2 * b];
+    v[1] += part[2 * b + 1];
+  }
+  block_sum(v, 2, red);
+  if (threadIdx.x == 0) *em = (float)(v[0] / v[1]);
+}
+
+__global__ void decorr_pad_kernel(const float* __restrict__ img, int h, int w, int N,
+                                  const float* __restrict__ emp, float* __restrict__ out) {
+  const float em = *emp;
+  const float fill = decorr_apodized(img, h, w, 0, 0, em);
+  const int ox = (N - w) / 2;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)N * N;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int yo = (int)(e / N), xo = (int)(e % N);
+    float v = fill;
+    if (yo < h && xo >= ox && xo < ox + w) v = decorr_apodized(img, h, w, yo, xo - ox, em);
+    out[e] = v;
+  }
+}
+
+// spectrum value at centred coordinates (ys, xs): natural index (+N/2 mod N);
+// the DC term reads 0 when zero_dc
+__device__ __forceinline__ float2 centred(const float2* F, int N, int ys, int xs, int zero_dc) {
+  const int yn = (ys + N / 2) % N, xn = (xs + N / 2) % N;
+  if (zero_dc && yn == 0 && xn == 0) return make_float2(0.f, 0.f);
+  return F[(size_t)yn * N + xn];
+}
+
+// sum of |F|^2 over the inscribed disc: blocks (split, image) -> partials
+constexpr int kDecSplits = 32;  // pixel-range splits per image (parallelism)
+__global__ void __launch_bounds__(256) decorr_cr_kernel(const float2* __restrict__ Fall, int N,
+                                                        int zero_dc, double* __restrict__ part) {
+  __shared__ double red[2 * 256];
+  const int z = blockIdx.y;
+  const float2* F = Fall + (size_t)z * N * N;
+  const double r2 = (double)N * N / 4;
+  const long long nn = (long long)N * N;
+  const long long e0 = nn * blockIdx.x / gridDim.x, e1 = nn * (blockIdx.x + 1) / gridDim.x;
+  double v[2] = {0, 0};
+  for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int ys = (int)(e / N), xs = (int)(e % N);
+    const int dy = ys - N / 2, dx = xs - N / 2;
+    if ((double)(dy * dy + dx * dx) < r2) {
+      const float2 f = centred(F, N, ys, xs, zero_dc);
+      v[0] += (double)__fadd_rn(__fmul_rn(f.x, f.x), __fmul_rn(f.y, f.y));
+    }
+  }
+  block_sum(v, 1, red);
+  if (threadIdx.x == 0) part[(size_t)z * gridDim.x + blockIdx.x] = v[0];
+}
+
+// the radial bin of every centred pixel for the band [crmin, crmax] (-1:
+// not visited): the reference's x-major walk over the centred square
+// (ox, ox + wb), stopping past x N + y = N^2/2 + N/2, bin
+// round(linmap(dist)) of the float32 distance; stored at y N + x
+__global__ void decorr_binmap_kernel(int N, float crmin, float crmax, int n_r,
+                                     int* __restrict__ bins) {
+  const int ox = (int)((float)N * (1.f - crmax) / 2.f);
+  const int wb = (int)((float)N * crmax);
+  const float kmax = (float)(N * N / 2 + N / 2);
+  const float span = __fsub_rn(crmax, crmin), top = (float)(n_r - 1);
+  const long long nn = (long long)N * N;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(e / N), x = (int)(e % N);
+    int bin = -1;
+    if (x >= ox && x < ox + wb && y >= ox && y < ox + wb && (float)(x * N + y) <= kmax) {
+      const int dx = x - N / 2, dy = y - N / 2;
+      float dist = (float)(dx * dx + dy * dy);
+      dist = (float)sqrt((double)__fdiv_rn(__fmul_rn(4.f, dist), (float)N * (float)N));
+      if (dist >= 0.f && dist <= crmax) {
+        float m = __fmul_rn(__fdiv_rn(__fsub_rn(dist, crmin), span), top);
+        if (m < 0.f) m = 0.f;
+        const int d = (int)round((double)m);
+        if (d < n_r) bin = d;
+      }
+    }
+    bins[e] = bin;
+  }
+}
+
+// ring coefficients: blocks (bin, image, split) sum, over the pixels of their
+// bin, the float32 terms re * re/|F| + im * im/|F| and (re/|F|)^2 +
+// (im/|F|)^2 (|F| in float64 from the float32 power, as the reference)
+__global__ void __launch_bounds__(256) decorr_ring_kernel(const float2* __restrict__ Fall, int N,
+                                                          int zero_dc,
+                                                          const int* __restrict__ bins,
+                                                          double* __restrict__ part) {
+  __shared__ double red[2 * 256];
+  const int bin = blockIdx.x, z = blockIdx.y, sp = blockIdx.z;
+  const float2* F = Fall + (size_t)z * N * N;
+  const long long nn = (long long)N * N;
+  const long long e0 = nn * sp / gridDim.z, e1 = nn * (sp + 1) / gridDim.z;
+  double v[2] = {0, 0};
+  for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    if (__ldg(bins + e) != bin) continue;
+    const float2 f = centred(F, N, (int)(e / N), (int)(e % N), zero_dc);
+    const double mag = sqrt((double)__fadd_rn(__fmul_rn(f.x, f.x), __fmul_rn(f.y, f.y)));
+    float nr = 0.f, ni = 0.f;
+    if (mag != 0.0) {
+      nr = (float)((double)f.x / mag);
+      ni = (float)((double)f.y / mag);
+    }
+    v[0] += (double)__fadd_rn(__fmul_rn(f.x, nr), __fmul_rn(f.y, ni));
+    v[1] += (double)__fadd_rn(__fmul_rn(nr, nr), __fmul_rn(ni, ni));
+  }
+  block_sum(v, 2, red);
+  if (threadIdx.x == 0) {
+    const size_t o = (((size_t)z * gridDim.x + bin) * gridDim.z + sp) * 2;
+    part[o] = v[0];
+    part[o + 1] = v[1];
+  }
+}
+
+// per image: cr and the 2 n_r coefficients from the split partials, in order
+__global__ void decorr_finish_kernel(const double* __restrict__ crp, int cr_splits,
+                                     const double* __restrict__ ringp, int n_r, int splits,
+                                     double* __restrict__ cr, double* __restrict__ coef) {
+  const int z = blockIdx.x;
+  for (int t = threadIdx.x; t <= n_r; t += blockDim.x) {
+    if (t == n_r) {
+      double c = 0;
+      for (int k = 0; k < cr_splits; ++k) c += crp[(size_t)z * cr_splits + k];
+      cr[z] = c;
+    } else {
+      double a = 0, b = 0;
+      for (int k = 0; k < splits; ++k) {
+        const size_t o = (((size_t)z * n_r + t) * splits + k) * 2;
+        a += ringp[o];
+        b += ringp[o + 1];
+      }
+      coef[(size_t)z * 2 * n_r + t] = a;
+      coef[(size_t)z * 2 * n_r + n_r + t] = b;
+    }
+  }
+}
+
 BlurAxis blur_axis(double sigma, int radius, int n) {
   if (!(sigma > 1e-15)) return BlurAxis{1, 0, 0};  // scipy leaves the axis alone
   if (2LL * radius + 1 > 2LL * n) return BlurAxis{2 * n, 0, 1};
   return BlurAxis{2 * radius + 1, -radius, 0};
+}
+
+template <typename A>
+int run_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
+                   const double* sigma, const float* alpha, const float* beta, float* d_out,
+                   char* base, cudaStream_t s) {
+  const size_t plane = (size_t)H * W;
+  const size_t k = (size_t)std::min(n, kBlurBatch);  // images per launch
+  A* w0 = (A*)base;                                    // k x 2H weights, axis 0
+  A* w1 = w0 + k * 2 * H;                              // k x 2W weights, axis 1
+  float* mid = (float*)(base + ((k * (2 * (size_t)H + 2 * (size_t)W) * sizeof(double) + 255) /
+                                256) * 256);
+  for (int c0 = 0; c0 < n; c0 += kBlurBatch) {
+    BlurBatch b{};
+    b.n = std::min(kBlurBatch, n - c0);
+    b.affine = alpha != nullptr;
+    int max_taps0 = 1, max_taps1 = 1;
+    for (int i = 0; i < b.n; ++i) {
+      const int g = c0 + i;
+      b.src[i] = src_index ? src_index[g] : g;
+      b.sigma[i] = sigma[g];
+      b.radius[i] = sigma[g] > 1e-15 ? (int)(4.0 * sigma[g] + 0.5) : 0;
+      b.alpha[i] = alpha ? alpha[g] : 1.f;
+      b.beta[i] = beta ? beta[g] : 0.f;
+      b.ax[0][i] = blur_axis(sigma[g], b.radius[i], H);
+      b.ax[1][i] = blur_axis(sigma[g], b.radius[i], W);
+      max_taps0 = std::max(max_taps0, b.ax[0][i].taps);
+      max_taps1 = std::max(max_taps1, b.ax[1][i].taps);
+    }
+    gauss_weights_kernel<A><<<dim3(b.n, 2), 256, 0, s>>>(b, H, W, w0, w1);
+    NX_CUDA_TRY(cudaGetLastError());
+    const int staged0 = max_taps0 <= kStageTaps;
+    const size_t smem0 = staged0 ? kStageTaps * sizeof(A) +
+                                       (size_t)(kTileRows + max_taps0 - 1) * kTileCols * sizeof(float)
+                                 : 0;
+    blur_axis0_kernel<A><<<dim3((W + kTileCols - 1) / kTileCols, (H + kTileRows - 1) / kTileRows,
+                                b.n),
+                           dim3(kTileCols, 256 / kTileCols), smem0, s>>>(b, d_in, H, W, w0,
+                                                                         staged0, mid);
+    NX_CUDA_TRY(cudaGetLastError());
+    const size_t smem1 = ((size_t)max_taps1 + 3) / 4 * 4 * sizeof(A) +
+                         ((size_t)kRowTile + max_taps1 - 1) * sizeof(float);
+    const int staged1 = smem1 <= 48 * 1024;
+    blur_axis1_kernel<A><<<dim3((W + kRowTile - 1) / kRowTile, H, b.n), 256,
+                           staged1 ? smem1 : 0, s>>>(b, mid, H, W, w1, staged1,
+                                                     d_out + (size_t)c0 * plane);
+    NX_CUDA_TRY(cudaGetLastError());
+  }
+  return NX_OK;
 }
 
 }  // namespace
@@ -600,18 +880,20 @@ extern "C" {
 size_t nx_gaussian_blur_batch_workspace_bytes(int H, int W, int n) {
   if (H < 1 || W < 1 || n < 1) return 256;
   const size_t k = (size_t)std::min(n, kBlurBatch);
-  return 256 + ((k * (2 * (size_t)H + 2 * (size_t)W) * sizeof(float) + 255) / 256) * 256 +
+  return 256 + ((k * (2 * (size_t)H + 2 * (size_t)W) * sizeof(double) + 255) / 256) * 256 +
          k * H * W * sizeof(float);
 }
 
-int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
-                           const double* sigma, const float* alpha, const float* beta,
-                           float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+int nx_gaussian_blur_batch_ex(const float* d_in, int H, int W, int n, const int* src_index,
+                              const double* sigma, const float* alpha, const float* beta,
+                              int flags, float* d_out, void* d_ws, size_t ws_bytes,
+                              void* stream) {
   if (H < 1 || W < 1 || n < 0) return nx::set_error("need H, W >= 1, n >= 0"), NX_ERR_INVALID_ARG;
   if (n == 0) return NX_OK;
   if (!d_in || !d_out || !sigma) return nx::set_error("NULL pointer"), NX_ERR_INVALID_ARG;
   if ((alpha == nullptr) != (beta == nullptr))
     return nx::set_error("alpha and beta go together"), NX_ERR_INVALID_ARG;
+  if (flags & ~NX_BLUR_FLOAT64_SUMS) return nx::set_error("unknown blur flags"), NX_ERR_INVALID_ARG;
   if (!d_ws || ws_bytes < nx_gaussian_blur_batch_workspace_bytes(H, W, n)) {
     nx::set_error("workspace too small: need %zu bytes",
                   nx_gaussian_blur_batch_workspace_bytes(H, W, n));
@@ -621,50 +903,18 @@ int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* sr
     if (!(sigma[i] <= 1e7)) return nx::set_error("sigma must be <= 1e7"), NX_ERR_INVALID_ARG;
     if (src_index && src_index[i] < 0) return nx::set_error("negative image index"), NX_ERR_INVALID_ARG;
   }
-  cudaStream_t s = (cudaStream_t)stream;
-  const size_t plane = (size_t)H * W;
   char* base = (char*)d_ws + 256;
-  const size_t k = (size_t)std::min(n, kBlurBatch);  // images per launch
-  float* w0 = (float*)base;                            // k x 2H weights, axis 0
-  float* w1 = w0 + k * 2 * H;                          // k x 2W weights, axis 1
-  float* mid = (float*)(base + ((k * (2 * (size_t)H + 2 * (size_t)W) * sizeof(float) + 255) /
-                                256) * 256);
-  for (int c0 = 0; c0 < n; c0 += kBlurBatch) {
-    BlurBatch b{};
-    b.n = std::min(kBlurBatch, n - c0);
-    b.affine = alpha != nullptr;
-    int max_taps1 = 1;
-    for (int i = 0; i < b.n; ++i) {
-      const int g = c0 + i;
-      b.src[i] = src_index ? src_index[g] : g;
-      b.sigma[i] = sigma[g];
-      b.radius[i] = sigma[g] > 1e-15 ? (int)(4.0 * sigma[g] + 0.5) : 0;
-      b.alpha[i] = alpha ? alpha[g] : 1.f;
-      b.beta[i] = beta ? beta[g] : 0.f;
-      b.ax[0][i] = blur_axis(sigma[g], b.radius[i], H);
-      b.ax[1][i] = blur_axis(sigma[g], b.radius[i], W);
-      max_taps1 = std::max(max_taps1, b.ax[1][i].taps);
-    }
-    gauss_weights_kernel<<<dim3(b.n, 2), 256, 0, s>>>(b, H, W, w0, w1);
-    NX_CUDA_TRY(cudaGetLastError());
-    int max_taps0 = 1;
-    for (int i = 0; i < b.n; ++i) max_taps0 = std::max(max_taps0, b.ax[0][i].taps);
-    const int staged0 = max_taps0 <= kStageTaps;
-    const size_t smem0 =
-        staged0 ? (kStageTaps + (size_t)(kTileRows + max_taps0 - 1) * kTileCols) * sizeof(float)
-                : 0;
-    blur_axis0_kernel<<<dim3((W + kTileCols - 1) / kTileCols, (H + kTileRows - 1) / kTileRows,
-                             b.n),
-                        dim3(kTileCols, 256 / kTileCols), smem0, s>>>(b, d_in, H, W, w0, staged0,
-                                                                      mid);
-    NX_CUDA_TRY(cudaGetLastError());
-    const size_t smem1 = (((size_t)max_taps1 + 3) / 4 * 4 + kRowTile + max_taps1 - 1) * sizeof(float);
-    const int staged1 = smem1 <= 48 * 1024;
-    blur_axis1_kernel<<<dim3((W + kRowTile - 1) / kRowTile, H, b.n), 256, staged1 ? smem1 : 0,
-                        s>>>(b, mid, H, W, w1, staged1, d_out + (size_t)c0 * plane);
-    NX_CUDA_TRY(cudaGetLastError());
-  }
-  return NX_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  return (flags & NX_BLUR_FLOAT64_SUMS)
+             ? run_blur_batch<double>(d_in, H, W, n, src_index, sigma, alpha, beta, d_out, base, s)
+             : run_blur_batch<float>(d_in, H, W, n, src_index, sigma, alpha, beta, d_out, base, s);
+}
+
+int nx_gaussian_blur_batch(const float* d_in, int H, int W, int n, const int* src_index,
+                           const double* sigma, const float* alpha, const float* beta,
+                           float* d_out, void* d_ws, size_t ws_bytes, void* stream) {
+  return nx_gaussian_blur_batch_ex(d_in, H, W, n, src_index, sigma, alpha, beta, 0, d_out, d_ws,
+                                   ws_bytes, stream);
 }
 
 size_t nx_gaussian_blur_workspace_bytes(int H, int W) {
@@ -680,7 +930,8 @@ int nx_gaussian_blur(const float* d_in, int H, int W, double sigma, int affine, 
 
 size_t nx_moment_sums_workspace_bytes(int batch) {
   const size_t b = (size_t)std::max(batch, 1);
-  return 256 + b * kSumMaxBlocks * 4 * sizeof(double) + b * 2 * sizeof(double);
+  return 256 + b * kSumMaxBlocks * 4 * sizeof(double) + b * 2 * sizeof(double) +
+         b * 2 * sizeof(float);
 }
 
 int nx_moment_sums(const float* d_x, const float* d_y, long long n, int batch, double* d_sums,
@@ -695,12 +946,13 @@ int nx_moment_sums(const float* d_x, const float* d_y, long long n, int batch, d
   cudaStream_t s = (cudaStream_t)stream;
   double* part = (double*)((char*)d_ws + 256);                    // batch x blocks x 4
   double* means = part + (size_t)batch * kSumMaxBlocks * 4;       // batch x 2 (the sums)
+  float* fmeans = (float*)(means + (size_t)batch * 2);            // batch x 2
   const int nb = sum_blocks(n);
   moment_mean_kernel<<<dim3(nb, batch), 256, 0, s>>>(d_x, d_y, n, part);
   NX_CUDA_TRY(cudaGetLastError());
-  moment_mean_final_kernel<<<batch, 256, 0, s>>>(part, nb, means);
+  moment_mean_final_kernel<<<batch, 256, 0, s>>>(part, nb, n, means, fmeans);
   NX_CUDA_TRY(cudaGetLastError());
-  moment_centred_kernel<<<dim3(nb, batch), 256, 0, s>>>(d_x, d_y, n, means, part);
+  moment_centred_kernel<<<dim3(nb, batch), 256, 0, s>>>(d_x, d_y, n, fmeans, part);
   NX_CUDA_TRY(cudaGetLastError());
   moment_final_kernel<<<batch, 256, 0, s>>>(part, nb, n, means, d_sums);
   NX_CUDA_TRY(cudaGetLastError());
@@ -813,16 +1065,99 @@ int nx_frc_ring_sums(const nx_frc_plan* p, const float* d_img1, const float* d_i
     const int q = std::min(chunk, pairs - q0);
     fft_lines_kernel<<<dim3(N, 2 * q), kFftThreads, smem, s>>>(
         p->fft, p->tw, 0, d_img1 + (size_t)q0 * stride, d_img2 + (size_t)q0 * stride, stride,
-        pitch, r0, c0, p->taper, nullptr, T);
+        pitch, r0, c0, p->taper, nullptr, nullptr, T);
     NX_CUDA_TRY(cudaGetLastError());
     fft_lines_kernel<<<dim3(N, 2 * q), kFftThreads, smem, s>>>(
-        p->fft, p->tw, 1, nullptr, nullptr, 0, 0, 0, 0, p->taper, T, F);
+        p->fft, p->tw, 1, nullptr, nullptr, 0, 0, 0, 0, p->taper, nullptr, T, F);
     NX_CUDA_TRY(cudaGetLastError());
     double* out = d_sums + (size_t)q0 * rows * 4;
     NX_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)q * rows * 4 * sizeof(double), s));
     frc_ring_kernel<<<dim3(p->n_rings, q), 256, 0, s>>>(F, N, p->pos, p->ring_start, out);
     NX_CUDA_TRY(cudaGetLastError());
   }
+  return NX_OK;
+}
+
+size_t nx_decorr_prepare_workspace_bytes(int h, int w) {
+  (void)h;
+  (void)w;
+  return 256 + 2 * 1024 * sizeof(double) + 256;
+}
+
+int nx_decorr_prepare(const float* d_img, int h, int w, float* d_out, int N, void* d_ws,
+                      size_t ws_bytes, void* stream) {
+  if (h < 1 || w < 1 || N < h || N < w) return nx::set_error("bad decorrelation image shape"), NX_ERR_INVALID_ARG;
+  if (!d_img || !d_out) return nx::set_error("NULL pointer"), NX_ERR_INVALID_ARG;
+  if (!d_ws || ws_bytes < nx_decorr_prepare_workspace_bytes(h, w))
+    return nx::set_error("workspace too small"), NX_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  double* part = (double*)((char*)d_ws + 256);
+  float* em = (float*)(part + 2 * 1024);
+  const int nb = (int)std::min<long long>(1024, ((long long)h * w + 255) / 256);
+  decorr_edge_kernel<<<nb, 256, 0, s>>>(d_img, h, w, part);
+  NX_CUDA_TRY(cudaGetLastError());
+  decorr_edge_final_kernel<<<1, 256, 0, s>>>(part, nb, em);
+  NX_CUDA_TRY(cudaGetLastError());
+  const long long n = (long long)N * N;
+  decorr_pad_kernel<<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(
+      d_img, h, w, N, em, d_out);
+  NX_CUDA_TRY(cudaGetLastError());
+  return NX_OK;
+}
+
+size_t nx_decorr_coefs_workspace_bytes(const nx_frc_plan* p, int B, int n_r) {
+  if (!p || B < 1 || n_r < 1) return 256;
+  // spectra and transposes, the bin map, the split partials of cr and the rings
+  return 256 + (size_t)2 * B * p->N * p->N * sizeof(float2) +
+         ((size_t)p->N * p->N + 64) * sizeof(int) + 256 +
+         (size_t)B * kDecSplits * sizeof(double) +
+         (size_t)B * n_r * kDecSplits * 2 * sizeof(double);
+}
+
+int nx_decorr_coefs(const nx_frc_plan* p, const float* d_base, const float* d_sub, int B,
+                    int zero_dc, float crmin, float crmax, int n_r, double* d_cr,
+                    double* d_coef, void* d_ws, size_t ws_bytes, void* stream) {
+  if (!p) return nx::set_error("plan is NULL"), NX_ERR_INVALID_ARG;
+  if (B < 1 || B > 65535 || n_r < 2 || n_r > 65535)
+    return nx::set_error("need 1 <= B <= 65535, 2 <= n_r <= 65535"), NX_ERR_INVALID_ARG;
+  if (!d_base || !d_cr || !d_coef) return nx::set_error("NULL pointer"), NX_ERR_INVALID_ARG;
+  if (!(crmax > crmin) || !(crmax <= 1.f))
+    return nx::set_error("need crmin < crmax <= 1"), NX_ERR_INVALID_ARG;
+  if (!d_ws || ws_bytes < nx_decorr_coefs_workspace_bytes(p, B, n_r)) {
+    nx::set_error("workspace too small: need %zu bytes",
+                  nx_decorr_coefs_workspace_bytes(p, B, n_r));
+    return NX_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int N = p->N;
+  float2* T = (float2*)((char*)d_ws + 256);
+  float2* F = T + (size_t)B * N * N;
+  const int smem = 2 * N * (int)sizeof(float2);
+  // image z: d_base - d_sub[z] with a subtrahend, else d_base[z]
+  const long long nn = (long long)N * N;
+  const float* r0 = d_base;
+  const float* r1 = d_sub ? d_base : d_base + nn;
+  const long long stride = d_sub ? 0 : 2 * nn;
+  fft_lines_kernel<<<dim3(N, B), kFftThreads, smem, s>>>(p->fft, p->tw, 0, r0, r1, stride, N, 0,
+                                                         0, nullptr, d_sub, nullptr, T);
+  NX_CUDA_TRY(cudaGetLastError());
+  fft_lines_kernel<<<dim3(N, B), kFftThreads, smem, s>>>(p->fft, p->tw, 1, nullptr, nullptr, 0, 0,
+                                                         0, 0, nullptr, nullptr, T, F);
+  NX_CUDA_TRY(cudaGetLastError());
+  int* bins = (int*)(F + (size_t)B * N * N);
+  double* crp = (double*)(bins + (size_t)N * N + 64);
+  crp = (double*)(((uintptr_t)crp + 255) & ~(uintptr_t)255);
+  double* ringp = crp + (size_t)B * kDecSplits;
+  const unsigned nb = (unsigned)std::min<long long>((nn + 255) / 256, 4096);
+  decorr_binmap_kernel<<<nb, 256, 0, s>>>(N, crmin, crmax, n_r, bins);
+  NX_CUDA_TRY(cudaGetLastError());
+  decorr_cr_kernel<<<dim3(kDecSplits, B), 256, 0, s>>>(F, N, zero_dc, crp);
+  NX_CUDA_TRY(cudaGetLastError());
+  const int splits = (int)std::max<long long>(1, std::min<long long>(kDecSplits, nn / 4096));
+  decorr_ring_kernel<<<dim3(n_r, B, splits), 256, 0, s>>>(F, N, zero_dc, bins, ringp);
+  NX_CUDA_TRY(cudaGetLastError());
+  decorr_finish_kernel<<<B, 64, 0, s>>>(crp, kDecSplits, ringp, n_r, splits, d_cr, d_coef);
+  NX_CUDA_TRY(cudaGetLastError());
   return NX_OK;
 }
 

@@ -38,7 +38,7 @@ def _to_device(img) -> tuple[torch.Tensor, bool]:
 
 
 def gaussian_blur_batch(stack: torch.Tensor, sigmas, index=None, alpha=None,
-                       beta=None) -> torch.Tensor:
+                       beta=None, float64_sums: bool = False) -> torch.Tensor:
     """scipy.ndimage.gaussian_filter of images of a (B, H, W) CUDA float32 stack
     (mode 'reflect', truncate 4), each with its own sigma: output i blurs image
     ``index[i]`` (default i), of ``alpha[i] * x + beta[i]`` when given (float32)."""
@@ -58,11 +58,12 @@ def gaussian_blur_batch(stack: torch.Tensor, sigmas, index=None, alpha=None,
     if alpha is not None:
         al = (C.c_float * n)(*[float(v) for v in alpha])
         be = (C.c_float * n)(*[float(v) for v in beta])
-    N.check(L.nx_gaussian_blur_batch(stack.data_ptr(), H, W, n, C.cast(ix, C.c_void_p),
-                                     C.cast(sig, C.c_void_p),
-                                     C.cast(al, C.c_void_p) if al is not None else None,
-                                     C.cast(be, C.c_void_p) if be is not None else None,
-                                     out.data_ptr(), ws.data_ptr(), ws.numel(), stream_ptr()),
+    N.check(L.nx_gaussian_blur_batch_ex(stack.data_ptr(), H, W, n, C.cast(ix, C.c_void_p),
+                                        C.cast(sig, C.c_void_p),
+                                        C.cast(al, C.c_void_p) if al is not None else None,
+                                        C.cast(be, C.c_void_p) if be is not None else None,
+                                        1 if float64_sums else 0, out.data_ptr(),
+                                        ws.data_ptr(), ws.numel(), stream_ptr()),
             "Gaussian blur")
     return out
 
@@ -592,6 +593,13 @@ class ParameterSweep:
     def calculate_frc(self, im_odd, im_even) -> float:
         return FIRECalculator().calculate_fire_number(im_odd, im_even)
 
+    def _decorr_grid(self, rec_all):
+        """Decorrelation resolution of every pair's all-frames reconstruction
+        (the whole stack, as the reference's n_frames path also uses)."""
+        S, R = rec_all.shape[:2]
+        return np.array([[DecorrAnalysis().run_analysis(rec_all[s, r, 0]) for r in range(R)]
+                         for s in range(S)])
+
     def _fire_grid(self, rec_odd, rec_even):
         """FRC resolution of every (sensitivity, radius) pair, one batch."""
         S, R = rec_odd.shape[:2]
@@ -659,9 +667,6 @@ class ParameterSweep:
 
     def run(self, im, magnification: int, sensitivity_array: list, radius_array: list,
             temporal_correlation: str = "AVG", use_decorr: bool = False, n_frames=None):
-        if use_decorr:
-            raise NotImplementedError("decorrelation analysis (use_decorr=True) is not "
-                                      "available; the FRC score is")
         stack, _ = _to_device(im)
         if stack.ndim != 3:
             raise ValueError("the sweep takes a (T, H, W) stack")
@@ -682,7 +687,8 @@ class ParameterSweep:
                 RSP_map = np.asarray(em["rsp"], dtype=np.float64).reshape(S, R)
                 self.sigma_map = np.asarray(em["sigma"]).reshape(S, R)
             if self.doFRCMapping:
-                FRC_map = self._fire_grid(rec_odd, rec_even)
+                FRC_map = self._decorr_grid(rec_all) if use_decorr else \
+                    self._fire_grid(rec_odd, rec_even)
         else:
             n_slices = T // fpt + (1 if T % fpt else 0)
             for s in range(S):
@@ -700,7 +706,12 @@ class ParameterSweep:
                     if s == S - 1 and r == R - 1:
                         RSP_map = np.mean(slices, axis=0)
             if self.doFRCMapping:
-                FRC_map = self._fire_grid(rec_odd, rec_even)
+                if use_decorr:  # the whole stack's reconstruction, as the reference
+                    full = self.reconstructions(stack, magnification, list(sensitivity_array),
+                                                list(radius_array), temporal_correlation, 0)[0]
+                    FRC_map = self._decorr_grid(full)
+                else:
+                    FRC_map = self._fire_grid(rec_odd, rec_even)
             if not self.doErrorMapping:
                 RSP_map = np.zeros((S, R))
         self.RSP_map, self.FRC_map = RSP_map, FRC_map
@@ -770,3 +781,192 @@ def calculate_frc(frame_1, frame_2, pixel_size: float = 1, units: str = "pixel",
         plt.imshow(fc.plot_frc_curve())
         plt.show()
     return res
+
+
+# ---------------------------------------------------------------------------
+# decorrelation analysis (src/nanopyx/core/analysis/decorr.pyx:23-393)
+# ---------------------------------------------------------------------------
+def _d_curve32(cr, coef, n_r):
+    """d(k) = sqrt(2) D_k / (cr sqrt(C_k)) with D, C the running ring sums, in
+    the reference's float32 (nan where cr or C_k is 0, d(0) nan -> 0)."""
+    f32 = np.float32
+    D = np.cumsum(coef[:n_r].astype(np.float32), dtype=np.float32)
+    Cc = np.cumsum(coef[n_r:].astype(np.float32), dtype=np.float32)
+    crf = f32(np.sqrt(np.float64(f32(cr))))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        out = (np.sqrt(2.0) * D.astype(np.float64) /
+               (np.float64(crf) * np.sqrt(Cc.astype(np.float64)))).astype(np.float32)
+    out[(crf == 0) | (Cc == 0)] = np.nan
+    if np.isnan(out[0]):
+        out[0] = 0
+    return out
+
+
+def _argmax_from(arr, x1, x2):
+    i, v = x1, arr[x1]
+    for k in range(x1, x2):
+        if arr[k] > v:
+            i, v = k, arr[k]
+    return [i, v]
+
+
+def _argmin_from(arr, x1, x2):
+    i, v = x1, arr[x1]
+    for k in range(x1, x2):
+        if arr[k] < v:
+            i, v = k, arr[k]
+    return [i, v]
+
+
+def _d_corr_max(d, r1, r2, n_r):
+    """Peak of a decorrelation curve, walking back from a maximum at the last
+    point while it is not 0.001 above the following minimum (decorr.pyx:
+    216-246); returns (frequency, amplitude) in float32."""
+    f32 = np.float32
+    t = np.array(d, dtype=np.float32)
+    out = _argmax_from(t, 0, n_r)
+    length = len(t)
+    while out[0] == length - 1:
+        t[length - 1] = 0
+        length -= 1
+        if length == 0:
+            out = [0, f32(0)]
+            break
+        out = _argmax_from(t, 0, n_r)
+        tmin = _argmin_from(t, int(out[0]), length - 1)
+        if f32(t[int(out[0])] - tmin[1]) > f32(0.001):
+            break
+        t[int(out[0])] = tmin[1]
+        out[0] = length - 1
+    return f32(f32(r1) + f32(f32(f32(r2) - f32(r1)) * f32(out[0])) / f32(n_r - 1)), f32(out[1])
+
+
+def _best_and_max(kc, a):
+    best, gm_max = [0.0, 0.0, 0.0], np.float32(0)
+    top, kc_max = [0.0, 0.0, 0.0], np.float32(0)
+    for k in range(len(kc)):
+        g = np.float32(kc[k] * a[k])
+        if g > gm_max:
+            gm_max = g
+            best = [kc[k], a[k], k]
+        if kc[k] > kc_max:
+            kc_max = kc[k]
+            top = [kc[k], a[k], k]
+    return best, top
+
+
+class DecorrAnalysis:
+    """Image decorrelation analysis (Descloux et al.), the reference's
+    DecorrAnalysis (decorr.pyx:23-393): resolution = 2 pixel_size / kc_max.
+
+    The image-sized work -- edge apodisation and padding, the Gaussian
+    high-pass images (float64 sums rounded to float32, as scipy does: at the
+    smallest widths the high-pass image is an exact cancellation), their
+    spectra and ring sums -- runs on the GPU, the 2 x n_g high-pass images of
+    a refinement round in one batch; the curve maxima and the refinement of
+    the band run on the host in the reference's float32.  ``roi`` is accepted
+    and, as in the reference, does not change the result (the analysis uses
+    the whole image)."""
+
+    def __init__(self, rmin: float = 0, rmax: float = 1, n_r: int = 50, n_g: int = 10,
+                 pixel_size: float = 1, units: str = "pixel", roi: tuple = (0, 0, 0, 0)):
+        self.rmin = self.rmin2 = float(np.float32(rmin))
+        self.rmax = self.rmax2 = float(np.float32(rmax))
+        self.n_r, self.n_g = int(n_r), int(n_g)
+        self.pixel_size = float(np.float32(pixel_size))
+        self.units = units
+        self.x0, self.x1, self.y0, self.y1 = roi
+        self.d0 = np.zeros(self.n_r, np.float32)
+        self.d = np.zeros((self.n_r, 2 * self.n_g), np.float32)
+        self.kc = np.zeros(2 * self.n_g, np.float32)
+        self.a_g = np.zeros(2 * self.n_g, np.float32)
+        self.kc0 = self.a0 = self.kc_gm = self.agm = self.kc_max = self.a_max = 0.0
+        self.resolution = 0.0
+
+    def _coefs(self, plan, base, sub, B, zero_dc, crmin, crmax):
+        L = N.lib()
+        cr = torch.empty(B, dtype=torch.float64, device=base.device)
+        coef = torch.empty((B, 2 * self.n_r), dtype=torch.float64, device=base.device)
+        ws = workspace(L.nx_decorr_coefs_workspace_bytes(plan.handle, B, self.n_r), base.device)
+        N.check(L.nx_decorr_coefs(plan.handle, base.data_ptr(),
+                                  sub.data_ptr() if sub is not None else None, B,
+                                  1 if zero_dc else 0, float(crmin), float(crmax), self.n_r,
+                                  cr.data_ptr(), coef.data_ptr(), ws.data_ptr(), ws.numel(),
+                                  stream_ptr()), "decorrelation coefficients")
+        return cr.cpu().numpy(), coef.cpu().numpy()
+
+    def run_analysis(self, img):
+        f32 = np.float32
+        t, _ = _to_device(img)
+        if t.ndim != 2:
+            raise ValueError("decorrelation analysis takes a 2-D image")
+        h, w = t.shape
+        n = 1 << int(np.ceil(np.log(max(h, w)) / np.log(2.0)))
+        L = N.lib()
+        temp = torch.empty((n, n), dtype=torch.float32, device=t.device)
+        ws = workspace(L.nx_decorr_prepare_workspace_bytes(h, w), t.device)
+        N.check(L.nx_decorr_prepare(t.data_ptr(), h, w, temp.data_ptr(), n, ws.data_ptr(),
+                                    ws.numel(), stream_ptr()), "decorrelation image")
+        plan = _frc_plan(n)
+        n_r, n_g = self.n_r, self.n_g
+        cr, coef = self._coefs(plan, temp, None, 1, True, self.rmin, self.rmax)
+        self.d0 = _d_curve32(cr[0], coef[0], n_r)
+        self.kc0, self.a0 = _d_corr_max(self.d0, 0, 1, n_r)
+        g_max = f32(n // 2) if self.kc0 == 0 else f32(f32(2) / self.kc0)
+        g_min = f32(0.14)
+        crmin, crmax = f32(self.rmin), f32(self.rmax)
+        d_curve = np.zeros((n_r, 2 * n_g), np.float32)
+        for refine in range(2):
+            lg0, lg1 = np.log(np.float64(g_min)), np.log(np.float64(g_max))
+            sig = [float(np.exp(lg0 + (lg1 - lg0) * np.float64(f32(f32(k) / f32(n_g - 1)))))
+                   for k in range(n_g)]
+            blurred = gaussian_blur_batch(temp[None], sig, [0] * n_g, float64_sums=True)
+            crs, coefs = self._coefs(plan, temp, blurred, n_g, False, crmin, crmax)
+            kc, a = [], []
+            for k in range(n_g):
+                d_curve[:, refine * n_g + k] = _d_curve32(crs[k], coefs[k], n_r)
+                r = _d_corr_max(d_curve[:, refine * n_g + k], crmin, crmax, n_r)
+                kc.append(r[0])
+                a.append(r[1])
+                self.kc[k], self.a_g[k] = r
+            if refine == 0:
+                r0 = _d_corr_max(self.d0, crmin, crmax, n_r)
+                kc.append(r0[0])
+                a.append(r0[1])
+                self.kc[n_g], self.a_g[n_g] = r0
+                gm, mx = _best_and_max(kc, a)
+                crmin = f32(max(f32(np.float64(min(gm[0], mx[0])) - 0.05), f32(self.rmin)))
+                crmax = f32(min(f32(np.float64(max(gm[0], mx[0])) + 0.3), f32(self.rmax)))
+                self.rmin2, self.rmax2 = float(crmin), float(crmax)
+                ind1 = f32(min(gm[2], mx[2]) - 1)
+                ind2 = f32(max(gm[2], mx[2]))
+                if ind2 < n_g:
+                    g_temp = f32(np.exp(lg0 + (lg1 - lg0) * np.float64(f32(ind1 / f32(n_g - 1)))))
+                    g_max = f32(np.exp(lg0 + (lg1 - lg0) * np.float64(f32(ind2 / f32(n_g - 1)))))
+                    g_min = g_temp
+                else:
+                    g_max = g_min
+                    g_min = f32(2 / n)
+            else:
+                gm, mx = _best_and_max(kc, a)
+                self.kc_gm, self.agm = float(gm[0]), float(gm[1])
+                self.kc_max, self.a_max = float(mx[0]), float(mx[1])
+        self.d = d_curve
+        with np.errstate(divide="ignore"):
+            # every kc 0: the reference divides by a value it never set (its
+            # result varies run to run); here 2 pixel_size / 0 = inf
+            self.resolution = float(f32(2) * f32(self.pixel_size) / f32(self.kc_max)) \
+                if self.kc_max else float("inf")
+        return self.resolution
+
+
+def calculate_decorr_analysis(frame, rmin: float = 0.0, rmax: float = 1.0, n_r: int = 50,
+                              n_g: int = 10, pixel_size: float = 1, units: str = "pixel",
+                              roi: tuple = (0, 0, 0, 0), plot_decorr_analysis: bool = False):
+    """Decorrelation resolution of a frame (methods/squirrel/resolution.py:47-104)."""
+    dc = DecorrAnalysis(rmin=rmin, rmax=rmax, n_r=n_r, n_g=n_g, pixel_size=pixel_size,
+                        units=units, roi=roi)
+    dc.run_analysis(frame)
+    if plot_decorr_analysis:
+        raise NotImplementedError("plotting needs matplotlib")
+    return dc.resolution

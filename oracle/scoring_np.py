@@ -195,3 +195,195 @@ def qnr(rsp, frc):
         k = 1 / (x0 - hi) * A1
         n = 1 / (np.exp(-k * (frc - x0)) + 1)
         return 2 * rsp * n / (rsp + n)
+
+
+# ---------------------------------------------------------------------------
+# decorrelation analysis (src/nanopyx/core/analysis/decorr.pyx:23-393 with
+# transform/edges.pyx:9-49, transform/normalize.pyx:13-29,
+# generate/mask.pyx:32-47, utils/array.pyx:8-40)
+# ---------------------------------------------------------------------------
+def apodize_edges(img):
+    """Cosine roll-off of the 20-pixel border towards the mean of the pixels
+    outside the inscribed circle of radius w/2 - 20."""
+    a = np.asarray(img, np.float32).astype(np.float64)
+    h, w = a.shape
+    off = 20
+    radius = np.float32(w // 2 - off)
+    yy, xx = np.meshgrid(np.arange(h), np.arange(w), indexing="ij")
+    dist = (yy - h // 2) ** 2 + (xx - w // 2) ** 2
+    sel = dist > float(radius) ** 2
+    edge_mean = a[sel].mean() if sel.any() else np.nan
+    x0 = np.abs(xx - w // 2).astype(np.float64)
+    y0 = np.abs(yy - h // 2).astype(np.float64)
+    ex, ey = np.abs(x0 - w // 2), np.abs(y0 - h // 2)
+    near = (ex <= off) | (ey <= off)
+    d = np.minimum(ex, ey)
+    c = (np.cos(d * np.pi / off - np.pi) + 1) / 2
+    out = a.copy()
+    out[near] = (c * (a - edge_mean) + edge_mean)[near]
+    far = ~near & (np.abs(xx - w // 2) > w // 2) & (np.abs(yy - h // 2) > h // 2)
+    out[far] = edge_mean
+    return out
+
+
+def decorr_pad(img):
+    """The power-of-two square filled with the first pixel, the image placed at
+    column (N - w) // 2 and row 0 (the reference's copy loop keeps the row
+    offset at 0)."""
+    a = np.asarray(img, np.float64)
+    h, w = a.shape
+    n = int(2 ** np.ceil(np.log(max(h, w)) / np.log(2.0)))
+    out = np.full((n, n), a.ravel()[0])
+    ox = (n - w) // 2
+    out[:h, ox:ox + w] = a
+    return out
+
+
+def _decorr_coefs(img, crmin, crmax, n_r, zero_dc=False):
+    """cr and the ring coefficients of one square image."""
+    n = img.shape[0]
+    F = np.fft.fftshift(np.fft.fft2(img))
+    if zero_dc:
+        F[n // 2, n // 2] = 0
+    mag = np.abs(F)
+    yy, xx = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    mask = ((yy - n / 2) ** 2 + (xx - n / 2) ** 2) < n * n / 4
+    cr = np.sqrt(np.sum(mag[mask] ** 2))
+    f32 = np.float32
+    ox = int(f32(n) * (f32(1) - f32(crmax)) / f32(2))
+    w = int(f32(n) * f32(crmax))
+    coef = np.zeros(2 * n_r)
+    kmax = n * n // 2 + n // 2
+    xs, ys = np.meshgrid(np.arange(ox, ox + w), np.arange(ox, ox + w), indexing="ij")
+    xs, ys = xs.ravel(), ys.ravel()  # x-major: the reference's loop order
+    keep = (xs * n + ys) <= kmax
+    xs, ys = xs[keep], ys[keep]
+    dist = np.sqrt(4.0 * ((xs - n // 2) ** 2 + (ys - n // 2) ** 2) / (n * n))
+    ok = dist <= crmax
+    xs, ys, dist = xs[ok], ys[ok], dist[ok]
+    dm = (dist - crmin) / (crmax - crmin) * (n_r - 1)
+    dm = np.maximum(dm, 0)
+    d = np.floor(dm + 0.5).astype(np.int64)
+    ok = d < n_r
+    xs, ys, d = xs[ok], ys[ok], d[ok]
+    m = mag[ys, xs]
+    np.add.at(coef, d, m)
+    np.add.at(coef, d + n_r, (m != 0).astype(np.float64))
+    return cr, coef
+
+
+def _d_curve(cr, coef, n_r):
+    D = np.cumsum(coef[:n_r])
+    Cc = np.cumsum(coef[n_r:])
+    with np.errstate(invalid="ignore", divide="ignore"):
+        out = np.where((cr == 0) | (Cc == 0), np.nan, np.sqrt(2) * D / (cr * np.sqrt(Cc)))
+    if np.isnan(out[0]):
+        out[0] = 0
+    return out
+
+
+def _get_max(arr, x1, x2):
+    i, v = x1, arr[x1]
+    for k in range(x1, x2):
+        if arr[k] > v:
+            i, v = k, arr[k]
+    return [i, v]
+
+
+def _get_min(arr, x1, x2):
+    i, v = x1, arr[x1]
+    for k in range(x1, x2):
+        if arr[k] < v:
+            i, v = k, arr[k]
+    return [i, v]
+
+
+def _d_corr_max(d, r1, r2, n_r):
+    t = np.array(d, dtype=np.float64)
+    out = _get_max(d, 0, n_r)
+    length = len(t)
+    dt = 0.001
+    while out[0] == length - 1:
+        t[length - 1] = 0
+        length -= 1
+        if length == 0:
+            out = [0, 0]
+            break
+        out = _get_max(t, 0, n_r)
+        tmin = _get_min(t, int(out[0]), length - 1)
+        if t[int(out[0])] - tmin[1] > dt:
+            break
+        t[int(out[0])] = tmin[1]
+        out[0] = length - 1
+    return [r1 + (r2 - r1) * out[0] / (n_r - 1), out[1]]
+
+
+def _scores(kc, a):
+    best, gm_max = [0.0, 0.0, 0.0], 0.0
+    for k in range(len(kc)):
+        if kc[k] * a[k] > gm_max:
+            gm_max = kc[k] * a[k]
+            best = [kc[k], a[k], k]
+    top, kc_max = [0.0, 0.0, 0.0], 0.0
+    for k in range(len(kc)):
+        if kc[k] > kc_max:
+            kc_max = kc[k]
+            top = [kc[k], a[k], k]
+    return best, top
+
+
+def decorr_resolution(img, rmin=0.0, rmax=1.0, n_r=50, n_g=10, pixel_size=1.0):
+    """DecorrAnalysis(...).run_analysis(img).resolution.  Sums and spectra in
+    float64; the padded image, its Gaussian blurs and the high-pass
+    differences in float32 as the reference forms them -- at the smallest blur
+    widths the high-pass image is a cancellation (the float32 blur equals the
+    image), and the decisions that follow depend on it -- and the search
+    state (band limits, blur widths) in float32."""
+    from scipy.ndimage import gaussian_filter
+
+    f32 = np.float32
+    temp = decorr_pad(apodize_edges(img)).astype(np.float32)
+    n = temp.shape[0]
+    cr, coef = _decorr_coefs(temp.astype(np.float64), rmin, rmax, n_r, zero_dc=True)
+    d0 = _d_curve(cr, coef, n_r).astype(np.float32)
+    kc0 = f32(_d_corr_max(d0, 0, 1, n_r)[0])
+    g_max = f32(n // 2) if kc0 == 0 else f32(f32(2) / kc0)
+    g_min = f32(0.14)
+    crmin, crmax = f32(rmin), f32(rmax)
+    kc_max = f32(0)
+
+    def widths(lo, hi):
+        return [float(np.exp(np.log(np.float64(lo)) + (np.log(np.float64(hi)) - np.log(np.float64(lo))) *
+                             np.float64(f32(f32(k) / f32(n_g - 1))))) for k in range(n_g)]
+
+    for refine in range(2):
+        curves = []
+        for sig in widths(g_min, g_max):
+            hp = (temp - gaussian_filter(temp, sig)).astype(np.float32)
+            c_, coef_ = _decorr_coefs(hp.astype(np.float64), float(crmin), float(crmax), n_r)
+            curves.append(_d_curve(c_, coef_, n_r).astype(np.float32))
+        res = [_d_corr_max(c, float(crmin), float(crmax), n_r) for c in curves]
+        kc = [f32(r[0]) for r in res]
+        a = [f32(r[1]) for r in res]
+        if refine == 0:
+            r0 = _d_corr_max(d0, float(crmin), float(crmax), n_r)
+            kc.append(f32(r0[0]))
+            a.append(f32(r0[1]))
+            gm, mx = _scores(kc, a)
+            crmin = f32(max(f32(np.float64(min(gm[0], mx[0])) - 0.05), f32(rmin)))
+            crmax = f32(min(f32(np.float64(max(gm[0], mx[0])) + 0.3), f32(rmax)))
+            ind1 = f32(min(gm[2], mx[2]) - 1)
+            ind2 = f32(max(gm[2], mx[2]))
+            if ind2 < n_g:
+                lg0, lg1 = np.log(np.float64(g_min)), np.log(np.float64(g_max))
+                g_temp = f32(np.exp(lg0 + (lg1 - lg0) * np.float64(f32(ind1 / f32(n_g - 1)))))
+                g_max = f32(np.exp(lg0 + (lg1 - lg0) * np.float64(f32(ind2 / f32(n_g - 1)))))
+                g_min = g_temp
+            else:
+                g_max = g_min
+                g_min = f32(2 / n)
+        else:
+            gm, mx = _scores(kc, a)
+            kc_max = f32(mx[0])
+    with np.errstate(divide="ignore"):
+        return float(f32(2) * f32(pixel_size) / kc_max) if kc_max else float("inf")

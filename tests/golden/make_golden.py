@@ -33,6 +33,9 @@ ESRRF_ST_CASES = [
 # eSRRF-3D: (magnification_xy, magnification_z, radius, sensitivity, mode, intensity weighting)
 ESRRF3D_CASES = [(2, 2, 1.5, 1, "average", 1), (3, 1, 1.0, 2, "std", 1), (2, 3, 2.0, 1, "average", 0),
                  (1, 2, 1.5, 1, "average", 1)]
+# decorrelation analysis of eSRRF reconstructions: (T, H, W, magnification, seed)
+DECORR_CASES = [(10, 32, 32, 2, 1), (10, 40, 50, 2, 2), (20, 64, 64, 2, 3), (8, 48, 48, 3, 4),
+                (6, 60, 45, 3, 5)]
 # scoring: (magnification, radius, sensitivity, ErrorMap fixedSigma)
 SCORE_CASES = [(2, 1.5, 1, 0), (4, 1.0, 2, 0), (2, 2.0, 1, 1)]
 
@@ -186,6 +189,20 @@ def main():
     g["score/sweep/qnr_nframes4"] = np.asarray(
         R["ParameterSweep"]().run(xq, 2, [1, 2], [1.0, 1.5], n_frames=4))
 
+    # decorrelation analysis (decorr.pyx) on reconstructions, and the sweep scored by it
+    dec = []
+    for k, (T, h, w, m, seed) in enumerate(DECORR_CASES):
+        xd = blinking_stack(T, h, w, 8, seed=seed)
+        rec = np.mean(np.asarray(R["eSRRF_ST"](verbose=False).run(
+            xd, magnification=m, radius=1.5, sensitivity=1, run_type="Threaded")), axis=0)
+        g[f"score/decorr/{k}/image"] = rec
+        dc = R["DecorrAnalysis"]()
+        dc.run_analysis(rec)
+        dec.append(dc.resolution)
+    g["score/decorr/resolution"] = np.array(dec, dtype=np.float64)
+    g["score/sweep/qnr_decorr"] = np.asarray(
+        R["ParameterSweep"]().run(xq, 2, [1, 2], [1.0, 1.5], use_decorr=True))
+
     # eSRRF-3D (_le_esrrf3d.pyx, eSRRF3D_workflow.py)
     x3 = (np.random.default_rng(24).random((5, 6, 14, 12)) * 100 + 10).astype(np.float32)
     g["esrrf3d/input"] = x3
@@ -204,7 +221,8 @@ def main():
 
     keep64 = ("esrrf_st/cases",)
     g = {k: (np.asarray(v, dtype=np.float32) if k not in keep64 and "/vals" not in k
-             and not k.startswith("score/sweep/qnr") else np.asarray(v)) for k, v in g.items()}
+             and not k.startswith("score/sweep/qnr") and k != "score/decorr/resolution"
+             else np.asarray(v)) for k, v in g.items()}
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT}: {len(g)} arrays, {os.path.getsize(OUT) / 1e6:.2f} MB")
 

@@ -41,9 +41,6 @@ def test_unimplemented_options_raise():
         nx.fht_space_interpolation(np.zeros((2, 4, 4), np.float32), 2, tile_size=128)
     with pytest.raises(NotImplementedError):
         nx.fht_space_interpolation(np.zeros((2, 4, 4), np.float32), 2, doMirrorPadding=False)
-    # the sweep scores by FRC; the decorrelation score is not built
-    with pytest.raises(NotImplementedError):
-        nx.run_esrrf_parameter_sweep(np.zeros((2, 4, 4), np.float32), use_decorr=True)
 
 
 class _Add(LiquidEngine):

@@ -205,3 +205,25 @@ def test_oracle_esrrf3d_st(golden, k):
 def test_oracle_esrrf3d_workflow(golden):
     got = O.esrrf3d(golden["esrrf3d/input"], 2, 2, 1.5, frames_per_timepoint=2)
     assert rel_err(got, golden["esrrf3d/workflow"]) <= 1e-5
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_oracle_decorrelation_resolution(golden, k):
+    from oracle import scoring_np as S
+
+    got = S.decorr_resolution(golden[f"score/decorr/{k}/image"])
+    assert abs(got - golden["score/decorr/resolution"][k]) <= 1e-6 * got
+
+
+def test_oracle_qnr_of_the_sweep_with_decorrelation(golden):
+    from oracle import scoring_np as S
+
+    xq = golden["score/sweep/input"]
+    rsp = np.zeros((2, 2))
+    res = np.zeros((2, 2))
+    for si, s in enumerate([1, 2]):
+        for ri, r in enumerate([1.0, 1.5]):
+            rec = O.esrrf_st(xq, 2, r, s).mean(0)
+            rsp[si, ri] = S.error_map(np.mean(xq, 0), rec)["rsp"]
+            res[si, ri] = S.decorr_resolution(rec.astype(np.float32))
+    assert np.abs(S.qnr(rsp, res) - golden["score/sweep/qnr_decorr"]).max() <= 1e-5
