@@ -173,7 +173,22 @@ __global__ void __launch_bounds__(256) blur_axis0_kernel(const __grid_constant__
     }
     __syncthreads();
     const float* col = tile + ty * kRowsPerThread * kTileCols + tx;
-    for (int j = 0; j < ax.taps; ++j) {
+    // 8 taps at a time from a 16-value window of the column: each staged
+    // value is read once per 8 taps instead of once per tap and output row
+    // (the tap order of every output is unchanged)
+    int j = 0;
+    for (; j + 8 <= ax.taps; j += 8) {
+      float win[16];
+#pragma unroll
+      for (int u = 0; u < 15; ++u) win[u] = col[(j + u) * kTileCols];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const A wj = ws[j + u];
+#pragma unroll
+        for (int q = 0; q < kRowsPerThread; ++q) acc[q] = mac(wj, win[q + u], acc[q]);
+      }
+    }
+    for (; j < ax.taps; ++j) {
       const A wj = ws[j];
 #pragma unroll
       for (int q = 0; q < kRowsPerThread; ++q) acc[q] = mac(wj, col[(q + j) * kTileCols], acc[q]);
@@ -284,12 +299,12 @@ __global__ void __launch_bounds__(256) moment_mean_kernel(const float* __restric
   for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n;
        i0 += stride * kSumRun) {
     float sx = 0.f, sy = 0.f;
-    for (int k = 0; k < kSumRun; ++k) {
+#pragma unroll 8
+    for (int k = 0; k < kSumRun; ++k) {  // unrolled: the loads of a run in flight together
       const long long i = i0 + k * stride;
-      if (i < n) {
-        sx += xs[i];
-        sy += y[i];
-      }
+      const float a = i < n ? __ldg(xs + i) : 0.f, b = i < n ? __ldg(y + i) : 0.f;
+      sx += a;
+      sy += b;
     }
     v[0] += sx;
     v[1] += sy;
@@ -337,16 +352,15 @@ __global__ void __launch_bounds__(256) moment_centred_kernel(const float* __rest
   for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n;
        i0 += stride * kSumRun) {
     float cxx = 0.f, cxy = 0.f, cyy = 0.f, dd = 0.f;
-    for (int k = 0; k < kSumRun; ++k) {
+#pragma unroll 8
+    for (int k = 0; k < kSumRun; ++k) {  // out-of-range terms are (mean, mean): they add 0
       const long long i = i0 + k * stride;
-      if (i < n) {
-        const float a = xs[i], b = y[i];
-        const float dx = a - mx, dy = b - my, d = __fsub_rn(a, b);
-        cxx = fmaf(dx, dx, cxx);
-        cxy = fmaf(dx, dy, cxy);
-        cyy = fmaf(dy, dy, cyy);
-        dd = fmaf(d, d, dd);
-      }
+      const float a = i < n ? __ldg(xs + i) : mx, b = i < n ? __ldg(y + i) : my;
+      const float dx = a - mx, dy = b - my, d = i < n ? __fsub_rn(a, b) : 0.f;
+      cxx = fmaf(dx, dx, cxx);
+      cxy = fmaf(dx, dy, cxy);
+      cyy = fmaf(dy, dy, cyy);
+      dd = fmaf(d, d, dd);
     }
     v[0] += cxx;
     v[1] += cxy;
@@ -672,7 +686,9 @@ __global__ void decorr_binmap_kernel(int N, float crmin, float crmax, int n_r,
     if (x >= ox && x < ox + wb && y >= ox && y < ox + wb && (float)(x * N + y) <= kmax) {
       const int dx = x - N / 2, dy = y - N / 2;
       float dist = (float)(dx * dx + dy * dy);
-      dist = (float)sqrt((double)__fdiv_rn(__fmul_rn(4.f, dist), (float)N * (float)N));
+      // the reference's double sqrt of a float, rounded to float, is the
+      // correctly rounded float sqrt
+      dist = __fsqrt_rn(__fdiv_rn(__fmul_rn(4.f, dist), (float)N * (float)N));
       if (dist >= 0.f && dist <= crmax) {
         float m = __fmul_rn(__fdiv_rn(__fsub_rn(dist, crmin), span), top);
         if (m < 0.f) m = 0.f;
