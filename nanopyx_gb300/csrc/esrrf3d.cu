@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "common.cuh"
 #include "internal.h"
@@ -56,17 +57,25 @@ __global__ void gradient3d_kernel(const float* __restrict__ v, int S, int H, int
 
 // one thread per output voxel inside the margins; gx/gy/gz/img: (S, Hm, Wm),
 // the xy-magnified volumes (slice zM of the z-magnified volume is slice
-// zM / mz of these)
+// zM / mz of these).  The window samples sit at whole input-pixel offsets
+// (i, j, k) from the voxel's centre, so their distance weights, validity
+// (distance != 0, xy distance <= tSO, signed z offset <= tSO_z) and inverse
+// distances depend on the offset alone: `tab` holds (weight, 1 / distance)
+// per offset, weight 0 where a sample does not count.  Per voxel only the
+// in-volume tests and the gradient indices use the voxel's float coordinates,
+// exactly as the reference forms them.
 __global__ void __launch_bounds__(256) rgc3d_kernel(const __grid_constant__ Rgc3d p,
                                                     const float* __restrict__ gx,
                                                     const float* __restrict__ gy,
                                                     const float* __restrict__ gz,
-                                                    const float* __restrict__ img, int frame,
+                                                    const float* __restrict__ img,
+                                                    const float2* __restrict__ tab, int frame,
                                                     float* __restrict__ out,
                                                     float* __restrict__ mean) {
   const int nx = p.Wm - 2 * p.margin, ny = p.Hm - 2 * p.margin, nz = p.Sm - 2 * p.margin_z;
   const long long n = (long long)nx * ny * nz;
   const size_t plane = (size_t)p.Hm * p.Wm;
+  const int nI = p.s1 - p.s0 + 1, nK = p.z1 - p.z0 + 1;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x) {
     const int cM = p.margin + (int)(e % nx);
@@ -79,42 +88,32 @@ __global__ void __launch_bounds__(256) rgc3d_kernel(const __grid_constant__ Rgc3
     for (int j = p.s0; j <= p.s1; ++j) {
       const float vy = __fadd_rn(yc, (float)j);
       if (!(0.f < vy && vy <= (float)(p.H - 1))) continue;
+      const size_t ry = (size_t)(int)__fmul_rn((float)p.mxy, vy) * p.Wm;
       for (int i = p.s0; i <= p.s1; ++i) {
         const float vx = __fadd_rn(xc, (float)i);
         if (!(0.f < vx && vx <= (float)(p.W - 1))) continue;
+        const size_t rxy = ry + (int)__fmul_rn((float)p.mxy, vx);
+        const float2* trow = tab + ((size_t)(j - p.s0) * nI + (i - p.s0)) * nK;
         for (int k = p.z0; k <= p.z1; ++k) {
+          const float2 t = __ldg(trow + (k - p.z0));
+          if (t.x == 0.f) continue;
           const float vz = __fadd_rn(zc, (float)k);
           if (!(0.f < vz && vz <= (float)(p.S - 1))) continue;
-          const float dx = __fsub_rn(vx, xc), dy = __fsub_rn(vy, yc), dz = __fsub_rn(vz, zc);
-          const float dxy2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-          const float dist = __fsqrt_rn(__fadd_rn(dxy2, __fmul_rn(dz, dz)));
-          const float dxy = __fsqrt_rn(dxy2);
-          if (!(dist != 0.f && dxy <= p.tSO && dz <= p.tSO_z)) continue;
-          const int zi = (int)__fmul_rn(vz, (float)p.mz);
-          const int yi = (int)__fmul_rn((float)p.mxy, vy);
-          const int xi = (int)__fmul_rn((float)p.mxy, vx);
-          const size_t li = (size_t)(zi / p.mz) * plane + (size_t)yi * p.Wm + xi;
+          const size_t li = (size_t)((int)__fmul_rn(vz, (float)p.mz) / p.mz) * plane + rxy;
           const float Gx = __ldg(gx + li), Gy = __ldg(gy + li), Gz = __ldg(gz + li);
-          const float wxy = expf(__fdiv_rn(-__fmul_rn(dxy, dxy), p.tSS));
-          const float wz = expf(__fdiv_rn(-__fmul_rn(dz, dz), p.tSS_z));
-          const float D = __fmul_rn(dist, __fmul_rn(wxy, wz));
-          const float D2 = __fmul_rn(D, D);
-          const float dw = __fmul_rn(D2, D2);
-          wsum = __fadd_rn(wsum, dw);
-          const float gdr =
-              __fadd_rn(__fadd_rn(__fmul_rn(Gx, dx), __fmul_rn(Gy, dy)), __fmul_rn(Gz, dz));
+          wsum = __fadd_rn(wsum, t.x);
+          const float fi = (float)i, fj = (float)j, fk = (float)k;
+          const float gdr = fmaf(Gz, fk, fmaf(Gy, fj, Gx * fi));
           if (gdr < 0.f) {
-            const float c1 = __fsub_rn(__fmul_rn(Gy, dz), __fmul_rn(Gz, dy));
-            const float c2 = __fsub_rn(__fmul_rn(Gz, dx), __fmul_rn(Gx, dz));
-            const float c3 = __fsub_rn(__fmul_rn(Gx, dy), __fmul_rn(Gy, dx));
-            const float num = __fadd_rn(__fadd_rn(__fmul_rn(c1, c1), __fmul_rn(c2, c2)),
-                                        __fmul_rn(c3, c3));
-            const float den = __fadd_rn(__fadd_rn(__fmul_rn(Gx, Gx), __fmul_rn(Gy, Gy)),
-                                        __fmul_rn(Gz, Gz));
-            float dk = __fdiv_rn(__fsqrt_rn(num), __fsqrt_rn(den));
-            if (isnan(dk)) dk = dist;
-            dk = __fsub_rn(1.f, __fdiv_rn(dk, dist));
-            rgc = __fadd_rn(rgc, __fmul_rn(dk, dw));
+            const float c1 = fmaf(Gy, fk, -Gz * fj);
+            const float c2 = fmaf(Gz, fi, -Gx * fk);
+            const float c3 = fmaf(Gx, fj, -Gy * fi);
+            const float num = fmaf(c3, c3, fmaf(c2, c2, c1 * c1));
+            const float den = fmaf(Gz, Gz, fmaf(Gy, Gy, Gx * Gx));
+            // |c| / |G| / distance; 0 / 0 (no gradient) counts as the distance
+            // itself in the reference, i.e. a zero contribution
+            const float dk = den > 0.f ? sqrtf(num) * rsqrtf(den) * t.y : 1.f;
+            rgc = fmaf(1.f - dk, t.x, rgc);
           }
         }
       }
@@ -126,12 +125,12 @@ __global__ void __launch_bounds__(256) rgc3d_kernel(const __grid_constant__ Rgc3
       rgc = 0.f;
     if (p.iw) rgc = __fmul_rn(rgc, __ldg(img + (size_t)(sM / p.mz) * plane + (size_t)rM * p.Wm + cM));
     const size_t o = ((size_t)sM * p.Hm + rM) * p.Wm + cM;
-    const float fi = (float)(frame + 1);
+    const float fr = (float)(frame + 1);
     if (p.mode == 0) {
-      out[o] = __fadd_rn(out[o], __fdiv_rn(__fsub_rn(rgc, out[o]), fi));
+      out[o] = __fadd_rn(out[o], __fdiv_rn(__fsub_rn(rgc, out[o]), fr));
     } else {
       const float delta = __fsub_rn(rgc, mean[o]);
-      mean[o] = __fadd_rn(mean[o], __fdiv_rn(delta, fi));
+      mean[o] = __fadd_rn(mean[o], __fdiv_rn(delta, fr));
       const float delta2 = __fsub_rn(rgc, mean[o]);
       out[o] = __fadd_rn(out[o], __fmul_rn(delta, delta2));
     }
@@ -157,6 +156,9 @@ using namespace nx;
 
 extern "C" {
 
+// window offsets per axis are at most 2 int(radius) + 2 <= kMaxWin
+constexpr int kMaxWin = 64;
+
 size_t nx_esrrf3d_workspace_bytes(int S, int H, int W, int magnification_xy,
                                   int magnification_z, int mode) {
   if (S < 1 || H < 1 || W < 1 || magnification_xy < 1 || magnification_z < 1) return 256;
@@ -164,7 +166,8 @@ size_t nx_esrrf3d_workspace_bytes(int S, int H, int W, int magnification_xy,
   const size_t volm = (size_t)S * H * magnification_xy * W * magnification_xy;
   const size_t out = volm * magnification_z;
   return 256 + rup(3 * (size_t)S * sizeof(float)) + rup(3 * vol * sizeof(float)) +
-         rup(4 * volm * sizeof(float)) + (mode ? rup(out * sizeof(float)) : 0);
+         rup(4 * volm * sizeof(float)) + (mode ? rup(out * sizeof(float)) : 0) +
+         rup((size_t)kMaxWin * kMaxWin * kMaxWin * sizeof(float2));
 }
 
 int nx_esrrf3d_st(const float* d_in, int T, int S, int H, int W, int magnification_xy,
@@ -212,6 +215,28 @@ int nx_esrrf3d_st(const float* d_in, int T, int S, int H, int W, int magnificati
   p.sensitivity = sensitivity;
   p.iw = do_intensity_weighting ? 1 : 0;
   p.mode = mode;
+  const int nI = p.s1 - p.s0 + 1, nK = p.z1 - p.z0 + 1;
+  if (nI > kMaxWin || nK > kMaxWin)
+    return nx::set_error("radius too large for the 3-D window"), NX_ERR_INVALID_ARG;
+  // per-offset (weight, 1 / distance), the reference's _c_calculate_dw3D
+  // (src/include/_c_sr_radial_gradient_convergence.c:96-102) at whole-pixel
+  // offsets; weight 0 where the sample does not count
+  std::vector<float2> tab((size_t)nI * nI * nK);
+  for (int j = p.s0; j <= p.s1; ++j)
+    for (int i = p.s0; i <= p.s1; ++i)
+      for (int k = p.z0; k <= p.z1; ++k) {
+        const double dxy2 = (double)i * i + (double)j * j;
+        const double d = std::sqrt(dxy2 + (double)k * k), dxy = std::sqrt(dxy2);
+        float w = 0.f, inv = 0.f;
+        if (d != 0 && dxy <= (double)p.tSO && (double)k <= (double)p.tSO_z) {
+          const float wxy = (float)std::exp(-dxy2 / (double)p.tSS);
+          const float wz = (float)std::exp(-(double)k * k / (double)p.tSS_z);
+          const float D = (float)(d * (double)(wxy * wz));
+          w = (float)std::pow((double)D, 4.0);
+          inv = (float)(1.0 / d);
+        }
+        tab[((size_t)(j - p.s0) * nI + (i - p.s0)) * nK + (k - p.z0)] = make_float2(w, inv);
+      }
   const size_t vol = (size_t)S * H * W;
   const size_t volm = (size_t)S * p.Hm * p.Wm;
   const long long nout = (long long)p.Sm * p.Hm * p.Wm;
@@ -223,6 +248,10 @@ int nx_esrrf3d_st(const float* d_in, int T, int S, int H, int W, int magnificati
   float* M = (float*)b;  // (4, S, Hm, Wm): image, gx, gy, gz magnified in xy
   b += rup(4 * volm * sizeof(float));
   float* mean = mode ? (float*)b : nullptr;
+  if (mode) b += rup((size_t)nout * sizeof(float));
+  float2* dtab = (float2*)b;
+  NX_CUDA_TRY(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(float2),
+                              cudaMemcpyHostToDevice, s));
   NX_CUDA_TRY(cudaMemsetAsync(zeros, 0, 3 * (size_t)S * sizeof(float), s));
   NX_CUDA_TRY(cudaMemsetAsync(d_out, 0, (size_t)nout * sizeof(float), s));
   if (mean) NX_CUDA_TRY(cudaMemsetAsync(mean, 0, (size_t)nout * sizeof(float), s));
@@ -253,7 +282,7 @@ int nx_esrrf3d_st(const float* d_in, int T, int S, int H, int W, int magnificati
       gz = G + 2 * vol;
     }
     if (ninner > 0) {
-      rgc3d_kernel<<<grid_of(ninner), 256, 0, s>>>(p, gx, gy, gz, img, f, d_out, mean);
+      rgc3d_kernel<<<grid_of(ninner), 256, 0, s>>>(p, gx, gy, gz, img, dtab, f, d_out, mean);
       NX_CUDA_TRY(cudaGetLastError());
     }
   }
