@@ -769,6 +769,8 @@ struct nx_esrrf_batch {
     std::vector<int> items;
     std::vector<int> unit_start;  // prefix sums, size n + 1
     size_t params_off, starts_off;
+    size_t jobs_off;      // the class's temporal finalisations (FinalizeJob list)
+    int n_jobs, job_blocks;
     int grid;
     nx::TmapPack maps;
   };
@@ -884,6 +886,20 @@ int nx_esrrf_batch_create(nx_esrrf_batch** out, const nx_esrrf_item* items, int 
       return NX_ERR_UNSUPPORTED;
     }
     cl.grid = std::min(cl.unit_start.back(), occ * sms);
+    // one finalisation job per item, timepoint and (AVG sweep) sensitivity
+    cl.n_jobs = 0;
+    long long blocks = 0;
+    for (int idx : cl.items) {
+      const auto& bi = b->items[idx];
+      const long long planeM = (long long)bi.desc.plan->rowsM * bi.desc.plan->colsM;
+      const int per_tp = bi.mode == kModeFull ? 1 : bi.n_out;
+      cl.n_jobs += bi.n_tp * per_tp;
+      blocks += (long long)bi.n_tp * per_tp * ((planeM + 255) / 256);
+    }
+    if (blocks > 0x7fffffffLL) { delete b; return invalid("batch too large for one launch"); }
+    cl.job_blocks = (int)blocks;
+    cl.jobs_off = off;
+    off += align256((size_t)cl.n_jobs * sizeof(FinalizeJob));
   }
   for (auto& bi : b->items) {
     const nx_esrrf_plan* p = bi.desc.plan;
@@ -956,6 +972,43 @@ int nx_esrrf_batch_bind(nx_esrrf_batch* b, void* d_ws, size_t ws_bytes, void* st
                                 params.size() * sizeof(FusedParams), cudaMemcpyHostToDevice, s));
     NX_CUDA_TRY(cudaMemcpyAsync(base + cl.starts_off, cl.unit_start.data(),
                                 cl.unit_start.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    std::vector<FinalizeJob> jobs;
+    jobs.reserve(cl.n_jobs);
+    int block0 = 0;
+    for (int idx : cl.items) {
+      const auto& bi = b->items[idx];
+      const nx_esrrf_plan* p = bi.desc.plan;
+      const long long planeM = (long long)p->rowsM * p->colsM;
+      const bool full = bi.mode == kModeFull;
+      const int F = full ? 5 : bi.n_out;
+      const float* rec = (const float*)(base + bi.rec_off);
+      const long long stride = (long long)bi.n_tp * planeM;
+      const int nblk = (int)((planeM + 255) / 256);
+      for (int tp = 0; tp < bi.n_tp; ++tp) {
+        const int nf = std::min(bi.fpt, bi.desc.T - tp * bi.fpt);
+        const int nch = std::min(bi.chunks, nf);
+        const float* rtp = rec + (size_t)tp * bi.chunks * F * planeM;
+        float* out = bi.desc.d_out + (size_t)tp * planeM;
+        for (int k = 0; k < (full ? 1 : bi.n_out); ++k) {
+          FinalizeJob j;
+          j.rec = full ? rtp : rtp + (size_t)k * planeM;
+          j.out = full ? out : out + (size_t)k * stride;
+          j.n = planeM;
+          j.out_stride = stride;
+          j.F = F;
+          j.nchunks = nch;
+          j.nf = nf;
+          j.corr_mask = full ? bi.desc.corr_mask : NX_CORR_AVG;
+          j.full = full ? 1 : 0;
+          j.block0 = block0;
+          block0 += nblk;
+          jobs.push_back(j);
+        }
+      }
+    }
+    if (!jobs.empty())
+      NX_CUDA_TRY(cudaMemcpyAsync(base + cl.jobs_off, jobs.data(), jobs.size() * sizeof(FinalizeJob),
+                                  cudaMemcpyHostToDevice, s));
   }
   NX_CUDA_TRY(cudaStreamSynchronize(s));
   b->d_ws = d_ws;
@@ -989,29 +1042,13 @@ int nx_esrrf_batch_launch(const nx_esrrf_batch* b, void* stream) {
     ut.ns_cap = cl.ns_cap;
     cudaError_t e = cl.entry->launch[cl.mode](ut, cl.maps, cl.grid, cs);
     if (e != cudaSuccess) return cuda_status(e, "batched eSRRF launch");
+    // every item's temporal finalisation of this class in one launch
+    e = launch_finalize_jobs((const FinalizeJob*)(base + cl.jobs_off), cl.n_jobs, cl.job_blocks,
+                             cs);
+    if (e != cudaSuccess) return cuda_status(e, "batched temporal finalize");
     for (int idx : cl.items) {
       const auto& bi = b->items[idx];
       const nx_esrrf_plan* p = bi.desc.plan;
-      const long long planeM = (long long)p->rowsM * p->colsM;
-      const bool full = bi.mode == kModeFull;
-      const int F = full ? 5 : bi.n_out;
-      const float* rec = (const float*)(base + bi.rec_off);
-      for (int tp = 0; tp < bi.n_tp; ++tp) {
-        const int nf = std::min(bi.fpt, bi.desc.T - tp * bi.fpt);
-        const int nch = std::min(bi.chunks, nf);
-        const float* rtp = rec + (size_t)tp * bi.chunks * F * planeM;
-        float* out = bi.desc.d_out + (size_t)tp * planeM;
-        const long long stride = (long long)bi.n_tp * planeM;
-        if (full) {
-          e = launch_finalize(rtp, F, nch, nf, planeM, bi.desc.corr_mask, out, stride, true, cs);
-        } else {
-          e = cudaSuccess;
-          for (int k = 0; k < bi.n_out && e == cudaSuccess; ++k)
-            e = launch_finalize(rtp + (size_t)k * planeM, F, nch, nf, planeM, NX_CORR_AVG,
-                                out + (size_t)k * stride, stride, false, cs);
-        }
-        if (e != cudaSuccess) return cuda_status(e, "batched temporal finalize");
-      }
       if (bi.desc.macro_pixel_correction) {
         e = launch_mpc(bi.desc.d_out, bi.n_out * bi.n_tp, p->rowsM, p->colsM, p->M,
                        (float*)(base + bi.mpc_off), cs);

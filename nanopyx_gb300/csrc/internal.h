@@ -80,6 +80,20 @@ cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n
                                 cudaStream_t s);
 // combine `nchunks` consecutive records (each F planes) of one timepoint with frame
 // counts derived from nf, and write the correlations of corr_mask to out[ci*out_stride]
+// one temporal finalisation of a batch: the chunk records of one timepoint
+// (rec, F fields, nchunks chunks over nf frames, n pixels) -> the output
+// planes at out (out_stride apart), VAR/TAC2/AVG per corr_mask, or the mean
+// only (!full); block0 = the job's first block in the launch
+struct FinalizeJob {
+  const float* rec;
+  float* out;
+  long long n, out_stride;
+  int F, nchunks, nf, corr_mask, full, block0;
+};
+// every job of a list in one launch (total_blocks = the last job's block0 +
+// its blocks)
+cudaError_t launch_finalize_jobs(const FinalizeJob* jobs, int njobs, int total_blocks,
+                                 cudaStream_t s);
 cudaError_t launch_finalize(const float* rec, int F, int nchunks, int nf, long long n,
                             int corr_mask, float* out, long long out_stride, bool full,
                             cudaStream_t s);

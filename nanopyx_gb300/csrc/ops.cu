@@ -389,11 +389,11 @@ __global__ void record_merge_kernel(float* __restrict__ acc, const float* __rest
 // Merges the `nchunks` consecutive records of one timepoint in frame order and
 // writes the correlations of corr_mask.  full: 5-field records; else one field
 // (the mean) per record.
-__global__ void finalize_kernel(const float* __restrict__ rec, int F, int nchunks, int nf,
-                                long long n, int corr_mask, float* __restrict__ out,
-                                long long out_stride, bool full) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
+__device__ __forceinline__ void finalize_pixel(const float* __restrict__ rec, int F,
+                                               int nchunks, int nf, long long n, int corr_mask,
+                                               float* __restrict__ out, long long out_stride,
+                                               bool full, long long i) {
+  {
     Moments a{0.f, 0.f, 0.f, 0.f, 0.f};
     int na = 0;
     for (int c = 0; c < nchunks; ++c) {
@@ -413,6 +413,31 @@ __global__ void finalize_kernel(const float* __restrict__ rec, int F, int nchunk
     }
     if (corr_mask & NX_CORR_TAC2) out[(ci++) * out_stride + i] = __fdiv_rn(a.c, fn - 1.f);
   }
+}
+
+__global__ void finalize_kernel(const float* __restrict__ rec, int F, int nchunks, int nf,
+                                long long n, int corr_mask, float* __restrict__ out,
+                                long long out_stride, bool full) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    finalize_pixel(rec, F, nchunks, nf, n, corr_mask, out, out_stride, full, i);
+}
+
+// a batch's finalisations in one launch: block -> job by binary search on
+// the jobs' first blocks, one pixel per thread
+__global__ void finalize_jobs_kernel(const FinalizeJob* __restrict__ jobs, int njobs) {
+  int lo = 0, hi = njobs - 1;
+  const int bx = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].block0 <= bx) lo = mid;
+    else hi = mid - 1;
+  }
+  const FinalizeJob j = jobs[lo];
+  const long long i = (long long)(bx - j.block0) * blockDim.x + threadIdx.x;
+  if (i < j.n)
+    finalize_pixel(j.rec, j.F, j.nchunks, j.nf, j.n, j.corr_mask, j.out, j.out_stride,
+                   j.full != 0, i);
 }
 
 // sr_temporal_correlations.py:46-75,205-221 on a resident stack, float32 and
@@ -812,6 +837,13 @@ cudaError_t launch_record_merge(float* acc, const float* blk, long long n, int n
                                 cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   record_merge_kernel<<<grid_for(n), kBlock, 0, s>>>(acc, blk, n, n_acc, n_blk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_jobs(const FinalizeJob* jobs, int njobs, int total_blocks,
+                                 cudaStream_t s) {
+  if (njobs == 0 || total_blocks == 0) return cudaSuccess;
+  finalize_jobs_kernel<<<total_blocks, kBlock, 0, s>>>(jobs, njobs);
   return cudaGetLastError();
 }
 

@@ -73,3 +73,17 @@ def test_cli_esrrf_end_to_end(tmp_path):
     ref = nx.eSRRF(x, magnification=4, temporal_correlation="VAR")
     got = tiff.imread(str(dst))
     assert got.shape == ref.shape and np.array_equal(got, ref)
+
+
+def test_esrrf3d_single_frame_and_margins_covering_the_volume():
+    """One frame; and a volume whose margins leave no inner voxel (all zero)."""
+    rng = np.random.default_rng(8)
+    x = (rng.random((1, 6, 20, 20)) * 100 + 10).astype(np.float32)
+    got = nx.eSRRF3D_ST(verbose=False).run(x, magnification_xy=2, magnification_z=2)
+    assert rel_err(got, O.esrrf3d_st(x, 2, 2)) <= TOL
+    y = (rng.random((2, 2, 8, 8)) * 100 + 10).astype(np.float32)
+    got = nx.eSRRF3D_ST(verbose=False).run(y, magnification_xy=1, magnification_z=1,
+                                           radius=1.5, PSF_ratio=2.8, voxel_ratio=4.0)
+    assert got.shape == (2, 8, 8)
+    assert np.array_equal(got, O.esrrf3d_st(y, 1, 1).astype(np.float32)) or \
+        rel_err(got, O.esrrf3d_st(y, 1, 1)) <= TOL

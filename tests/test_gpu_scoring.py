@@ -245,3 +245,31 @@ def test_cli_decorrelation_command(golden, tmp_path):
     assert cli.main(["linkinpy-Metrics-ImageDecorrelationAnalysis", str(src), str(dst)]) == 0
     val = float(dst.read_text().splitlines()[1].split(",")[1])
     assert abs(val - golden["score/decorr/resolution"][0]) <= 1e-5 * val
+
+
+def test_sweep_with_more_than_four_sensitivities_against_oracle():
+    """Five sensitivities: two sensitivity groups per radius in the batch."""
+    from oracle import esrrf_np as O
+
+    x = blinking_stack(6, 24, 24, 6, seed=41)
+    sens = [1, 1.5, 2, 3, 4]
+    ps = nx.ParameterSweep()
+    ps.run(x, 2, sens, [1.5])
+    for si, s in enumerate(sens):
+        rgc = O.esrrf_st(x, 2, 1.5, s)
+        rsp = S.error_map(np.mean(x, 0), rgc.mean(0))["rsp"]
+        frc = S.fire_number(rgc[1::2].mean(0), rgc[::2].mean(0))[0]
+        assert abs(ps.RSP_map[si, 0] - rsp) <= 1e-4
+        assert abs(ps.FRC_map[si, 0] - frc) <= 1e-3 * max(abs(frc), 1.0)
+
+
+def test_error_map_without_magnification_against_oracle():
+    """Reference and SR image of one size: no interpolation (error_map.pyx:54-57)."""
+    rng = np.random.default_rng(9)
+    ref = (rng.random((40, 36)) * 50 + 100).astype(np.float32)
+    sr = (ref + rng.standard_normal((40, 36)).astype(np.float32) * 3).astype(np.float32)
+    em = nx.ErrorMap()
+    em.optimise(ref, sr)
+    o = S.error_map(ref, sr)
+    assert abs(em.getRSP() - o["rsp"]) <= 1e-5
+    assert abs(em.getRSE() - o["rse"]) <= 1e-4 * o["rse"]
