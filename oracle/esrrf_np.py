@@ -1,7 +1,7 @@
 """FP64 NumPy restatement of the reference's eSRRF / SRRF CPU path.
 
 TEST INFRASTRUCTURE ONLY: the oracle.  Only ``tests/``, ``__graft_entry__.smoke``
-and ``bench.py``'s CPU-baseline legs import it, as the checker; the product
+and ``bench.py``'s CPU-baseline legs import it, to check results; the product
 package ``nanopyx_gb300`` never does.
 
 Every function restates, in float64 arithmetic, one reference routine (paths

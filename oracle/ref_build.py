@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in ``nanopyx_gb300`` imports this module;
 only ``tests/``, ``__graft_entry__`` (build/smoke) and the ``cpu_baseline`` /
-``--impl reference`` legs of ``bench.py`` use what it produces, as the checker
+``--impl reference`` legs of ``bench.py`` use what it produces, to check results
 and as the timed CPU baseline.
 
 Two stages, so that the compiled reference can also be produced on a machine

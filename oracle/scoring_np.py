@@ -1,7 +1,7 @@
 """Float64 NumPy/SciPy restatement of the parameter sweep's scoring.
 
 TEST INFRASTRUCTURE ONLY: the oracle.  Only ``tests/`` import it, as the
-checker; the product package ``nanopyx_gb300`` never does.
+reference for the results; the product package ``nanopyx_gb300`` never does.
 
 Each function restates one reference routine (paths inside the reference
 project), in float64 where the reference mixes precisions:

@@ -22,7 +22,7 @@ BLOCK = 12
 
 def load():
     assert ref_build.available() or ref_build.build(), \
-        "the compiled reference (oracle/_ref) is needed as the checker"
+        "the compiled reference (oracle/_ref) is needed for these comparisons"
     return ref_build.load()
 
 
