@@ -924,6 +924,11 @@ def bench_standalone_ops(dev, T=100):
         s.cuda_stream), "cr"))
     b = (x.numel() + out.numel()) * 4
     rows.append({"op": f"cr_shift_magnify {T}x512x512 m=5", "ms": ms, "gbs": b / ms / 1e6})
+    # write ceiling of that output: a library fill of the same buffer (torch's
+    # own kernel, not ours; reported only to bound the write-dominated op)
+    ms = timeit(lambda: out.fill_(1.0))
+    rows.append({"op": f"write-only fill of the {T}x2560x2560 output (torch fill_, ceiling)",
+                 "ms": ms, "gbs": out.numel() * 4 / ms / 1e6})
     for name, c in (("AVG", 1), ("VAR", 2), ("TAC2", 4)):
         ms = timeit(lambda: N.check(L.nx_temporal_correlation(
             stack.data_ptr(), T, H * m * W * m, c, res.data_ptr(), s.cuda_stream), "tc"))

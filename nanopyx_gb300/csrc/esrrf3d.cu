@@ -36,6 +36,11 @@ struct Rgc3d {
   int s0, s1, z0, z1;  // window offsets, inclusive
   float tSS, tSO, tSS_z, tSO_z, sensitivity;
   int iw, mode;
+  // floor(x / mz) = (x * mz_magic) >> 32 in 64-bit arithmetic for 0 <= x,
+  // x * mz < 2^32
+  // (mz_magic = floor(2^32 / mz) + 1: the excess x (mz_magic - 2^32 / mz) / 2^32
+  // stays below 1 / mz, so it never crosses the next integer)
+  unsigned long long mz_magic;
 };
 
 __global__ void gradient3d_kernel(const float* __restrict__ v, int S, int H, int W,
@@ -78,9 +83,17 @@ __global__ void __launch_bounds__(256) rgc3d_kernel(const __grid_constant__ Rgc3
   const int nI = p.s1 - p.s0 + 1, nK = p.z1 - p.z0 + 1;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
        e += (long long)gridDim.x * blockDim.x) {
-    const int cM = p.margin + (int)(e % nx);
-    const int rM = p.margin + (int)((e / nx) % ny);
-    const int sM = p.margin_z + (int)(e / ((long long)nx * ny));
+    int cM, rM, sM;
+    if (n < (1LL << 31)) {  // 32-bit index arithmetic
+      const unsigned u = (unsigned)e;
+      cM = p.margin + (int)(u % (unsigned)nx);
+      rM = p.margin + (int)((u / (unsigned)nx) % (unsigned)ny);
+      sM = p.margin_z + (int)(u / ((unsigned)nx * (unsigned)ny));
+    } else {
+      cM = p.margin + (int)(e % nx);
+      rM = p.margin + (int)((e / nx) % ny);
+      sM = p.margin_z + (int)(e / ((long long)nx * ny));
+    }
     const float xc = __fdiv_rn((float)cM, (float)p.mxy);
     const float yc = __fdiv_rn((float)rM, (float)p.mxy);
     const float zc = __fdiv_rn((float)sM, (float)p.mz);
@@ -99,7 +112,9 @@ __global__ void __launch_bounds__(256) rgc3d_kernel(const __grid_constant__ Rgc3
           if (t.x == 0.f) continue;
           const float vz = __fadd_rn(zc, (float)k);
           if (!(0.f < vz && vz <= (float)(p.S - 1))) continue;
-          const size_t li = (size_t)((int)__fmul_rn(vz, (float)p.mz) / p.mz) * plane + rxy;
+          // slice of the xy-magnified volumes: (int)(vz mz) / mz, vz > 0
+          const unsigned zm = (unsigned)(int)__fmul_rn(vz, (float)p.mz);
+          const size_t li = (size_t)((zm * p.mz_magic) >> 32) * plane + rxy;
           const float Gx = __ldg(gx + li), Gy = __ldg(gy + li), Gz = __ldg(gz + li);
           wsum = __fadd_rn(wsum, t.x);
           const float fi = (float)i, fj = (float)j, fk = (float)k;
@@ -197,6 +212,9 @@ int nx_esrrf3d_st(const float* d_in, int T, int S, int H, int W, int magnificati
   p.Hm = H * mxy;
   p.Wm = W * mxy;
   p.Sm = S * mz;
+  if ((unsigned long long)p.Sm * (unsigned long long)mz >= (1ULL << 32))
+    return nx::set_error("S * magnification_z^2 must be below 2^32"), NX_ERR_INVALID_ARG;
+  p.mz_magic = (1ULL << 32) / (unsigned long long)mz + 1;
   // the reference's scalars (_le_esrrf3d.pyx:73-86): radius and radius_z are
   // Python floats, sigma and the thresholds C floats
   const float sigma = (float)(radius / 2.355);

@@ -81,9 +81,14 @@ def test_esrrf3d_single_frame_and_margins_covering_the_volume():
     x = (rng.random((1, 6, 20, 20)) * 100 + 10).astype(np.float32)
     got = nx.eSRRF3D_ST(verbose=False).run(x, magnification_xy=2, magnification_z=2)
     assert rel_err(got, O.esrrf3d_st(x, 2, 2)) <= TOL
+    # radius_z = 1.0 * 2.0 / 2.0 = S / 2: accepted, and the z margin int(radius_z)
+    # = 1 leaves no inner slice, so every voxel stays 0
     y = (rng.random((2, 2, 8, 8)) * 100 + 10).astype(np.float32)
     got = nx.eSRRF3D_ST(verbose=False).run(y, magnification_xy=1, magnification_z=1,
-                                           radius=1.5, PSF_ratio=2.8, voxel_ratio=4.0)
+                                           radius=1.0, PSF_ratio=2.0, voxel_ratio=2.0)
     assert got.shape == (2, 8, 8)
-    assert np.array_equal(got, O.esrrf3d_st(y, 1, 1).astype(np.float32)) or \
-        rel_err(got, O.esrrf3d_st(y, 1, 1)) <= TOL
+    ref = O.esrrf3d_st(y, 1, 1, 1.0, 2.0, 2.0)
+    assert not np.any(ref) and np.array_equal(got, ref.astype(np.float32))
+    # one slice past that radius the reference declines (warning, None)
+    assert nx.eSRRF3D_ST(verbose=False).run(y, magnification_xy=1, magnification_z=1,
+                                            radius=1.5, PSF_ratio=2.8, voxel_ratio=4.0) is None
