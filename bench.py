@@ -383,7 +383,11 @@ def run_gpu_arm(args):
 
     # end to end through the public API with host buffers
     e2e_times = []
+    res = None
     for i in range(max(1, min(args.steps, 3)) + 1):
+        # the previous call's result (262 MB at the full size) is released
+        # before the clock starts, not inside the next call's timing
+        res = None
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         res = nx.eSRRF(stack_np, magnification=m, radius=R, sensitivity=s,
