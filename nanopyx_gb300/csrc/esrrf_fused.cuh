@@ -251,8 +251,12 @@ template <int M, int J, int TY, int FP, int NP>
 struct Producer {
   using G = Geo<M, J, TY, FP, NP>;
   float* inb;
-  float* gsm;  // plane 2 fr: gc, 2 fr + 1: gr
-  float* t1;   // plane 2 fr: gx, 2 fr + 1: gy (half-grid columns)
+  // Roberts-Cross gradients and the column pass's half-grid columns:
+  //   FP = 1: plane 0 gc / gx, plane 1 gr / gy;
+  //   FP >= 2: per frame pair pp one plane of float4 (gc, gc', gr, gr') /
+  //            (gx, gx', gy, gy'), so the passes run on packed frame pairs
+  float* gsm;
+  float* t1;
   float* hg0;  // slot 0; slot s at hg0 + s * S_HG
   float* ri0;  // slot s, frame fr at ri0 + (s * FP + fr) * S_RI
   const float* rw;
@@ -270,16 +274,25 @@ struct Producer {
       const int ib = (r - u.y_start) * G::BW + (c0 - u.x_start);   // image[r1][c0]
       const int id = (r0 - u.y_start) * G::BW + (c0 - u.x_start);  // image[r0][c0]
       const int ie = (r - u.y_start) * G::BW + (c - u.x_start);    // image[r1][c1]
+      float gc[FP], gr[FP];
 #pragma unroll
       for (int fr = 0; fr < FP; ++fr) {
-        float gc = 0.f, gr = 0.f;
+        gc[fr] = gr[fr] = 0.f;
         if (in) {
           const float a = tin[fr][ia], bb = tin[fr][ib], d = tin[fr][id], e = tin[fr][ie];
-          gc = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
-          gr = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
+          gc[fr] = __fsub_rn(__fadd_rn(__fsub_rn(a, bb), e), d);
+          gr[fr] = __fsub_rn(__fadd_rn(__fadd_rn(-a, bb), e), d);
         }
-        gsm[(2 * fr) * G::S_G + i] = gc;
-        gsm[(2 * fr + 1) * G::S_G + i] = gr;
+      }
+      if constexpr (FP >= 2) {
+        // frame pair pp: float4 (gc, gc', gr, gr') per position
+#pragma unroll
+        for (int pp = 0; pp < FP / 2; ++pp)
+          reinterpret_cast<float4*>(gsm)[pp * G::S_G + i] =
+              make_float4(gc[2 * pp], gc[2 * pp + 1], gr[2 * pp], gr[2 * pp + 1]);
+      } else {
+        gsm[i] = gc[0];
+        gsm[G::S_G + i] = gr[0];
       }
     }
     float* ri = ri0 + s * FP * G::S_RI;
@@ -303,7 +316,9 @@ struct Producer {
 
   // gradient column pass onto the half-grid columns
   // (each row's even half-grid columns first, then its odd ones, so that the
-  // lanes of a warp mostly take the same odd / even branch)
+  // lanes of a warp mostly take the same odd / even branch).  With frame
+  // pairs the planes hold float4 (x, x', y, y') per position and the taps run
+  // as packed f32x2 operations: the same IEEE operations per frame.
   __device__ void column_pass(const FusedParams& p, const UnitGeo& u) const {
     const int twoW = 2 * u.W;
     constexpr int HALF = (G::HG_C + 1) / 2;
@@ -312,49 +327,71 @@ struct Producer {
       const int kxl = j < HALF ? 2 * j : 2 * (j - HALF) + 1;
       const int o = rl * G::HG_C + kxl;
       const int kx = u.kb_x + kxl;
-      float vc[FP], vr[FP];
+      const bool valid = kx >= 1 && kx <= u.kmax_x;
+      if constexpr (FP >= 2) {
 #pragma unroll
-      for (int fr = 0; fr < FP; ++fr) vc[fr] = vr[fr] = 0.f;
-      if (kx >= 1 && kx <= u.kmax_x) {
-        if (kx >= twoW) {
+        for (int pp = 0; pp < FP / 2; ++pp) {
+          const float4* g4 = reinterpret_cast<const float4*>(gsm) + pp * G::S_G + rl * G::NCX;
+          float2 vc = make_float2(0.f, 0.f), vr = make_float2(0.f, 0.f);
+          if (valid) {
+            if (kx >= twoW) {
 #pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX;
-            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX;
+              for (int t = 0; t < 4; ++t) {
+                const float4 q = g4[p.cx_base + t - u.CX0];
+                const float2 w = make_float2(p.cx[t], p.cx[t]);
+                vc = __ffma2_rn(w, make_float2(q.x, q.y), vc);
+                vr = __ffma2_rn(w, make_float2(q.z, q.w), vr);
+              }
+            } else if (kx & 1) {
+              const float4 q = g4[((kx - 1) >> 1) - u.CX0];
+              vc = make_float2(q.x, q.y);
+              vr = make_float2(q.z, q.w);
+            } else {
+              const float4* g = g4 + (kx >> 1) - 2 - u.CX0;
+              const float2 c0 = make_float2(-0.0625f, -0.0625f);
+              const float2 c1 = make_float2(0.5625f, 0.5625f);
+              const float4 q0 = g[0], q1 = g[1], q2 = g[2], q3 = g[3];
+              vc = __fmul2_rn(c0, make_float2(q0.x, q0.y));
+              vr = __fmul2_rn(c0, make_float2(q0.z, q0.w));
+              vc = __ffma2_rn(c1, make_float2(q1.x, q1.y), vc);
+              vr = __ffma2_rn(c1, make_float2(q1.z, q1.w), vr);
+              vc = __ffma2_rn(c1, make_float2(q2.x, q2.y), vc);
+              vr = __ffma2_rn(c1, make_float2(q2.z, q2.w), vr);
+              vc = __ffma2_rn(c0, make_float2(q3.x, q3.y), vc);
+              vr = __ffma2_rn(c0, make_float2(q3.z, q3.w), vr);
+            }
+          }
+          reinterpret_cast<float4*>(t1)[pp * G::S_T1 + o] = make_float4(vc.x, vc.y, vr.x, vr.y);
+        }
+      } else {
+        const float* g0 = gsm + rl * G::NCX;
+        const float* g1 = gsm + G::S_G + rl * G::NCX;
+        float vc = 0.f, vr = 0.f;
+        if (valid) {
+          if (kx >= twoW) {
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
               const int cl = p.cx_base + t - u.CX0;
-              vc[fr] = fmaf(p.cx[t], g0[cl], vc[fr]);
-              vr[fr] = fmaf(p.cx[t], g1[cl], vr[fr]);
+              vc = fmaf(p.cx[t], g0[cl], vc);
+              vr = fmaf(p.cx[t], g1[cl], vr);
             }
-          }
-        } else if (kx & 1) {
-          const int cl = ((kx - 1) >> 1) - u.CX0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            vc[fr] = gsm[(2 * fr) * G::S_G + rl * G::NCX + cl];
-            vr[fr] = gsm[(2 * fr + 1) * G::S_G + rl * G::NCX + cl];
-          }
-        } else {
-          const int cl = (kx >> 1) - 2 - u.CX0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* g0 = gsm + (2 * fr) * G::S_G + rl * G::NCX + cl;
-            const float* g1 = gsm + (2 * fr + 1) * G::S_G + rl * G::NCX + cl;
-            float c = -0.0625f * g0[0], r = -0.0625f * g1[0];
-            c = fmaf(0.5625f, g0[1], c);
-            r = fmaf(0.5625f, g1[1], r);
-            c = fmaf(0.5625f, g0[2], c);
-            r = fmaf(0.5625f, g1[2], r);
-            vc[fr] = fmaf(-0.0625f, g0[3], c);
-            vr[fr] = fmaf(-0.0625f, g1[3], r);
+          } else if (kx & 1) {
+            const int cl = ((kx - 1) >> 1) - u.CX0;
+            vc = g0[cl];
+            vr = g1[cl];
+          } else {
+            const int cl = (kx >> 1) - 2 - u.CX0;
+            float c = -0.0625f * g0[cl], r = -0.0625f * g1[cl];
+            c = fmaf(0.5625f, g0[cl + 1], c);
+            r = fmaf(0.5625f, g1[cl + 1], r);
+            c = fmaf(0.5625f, g0[cl + 2], c);
+            r = fmaf(0.5625f, g1[cl + 2], r);
+            vc = fmaf(-0.0625f, g0[cl + 3], c);
+            vr = fmaf(-0.0625f, g1[cl + 3], r);
           }
         }
-      }
-#pragma unroll
-      for (int fr = 0; fr < FP; ++fr) {
-        t1[(2 * fr) * G::S_T1 + o] = vc[fr];
-        t1[(2 * fr + 1) * G::S_T1 + o] = vr[fr];
+        t1[o] = vc;
+        t1[G::S_T1 + o] = vr;
       }
     }
   }
@@ -366,54 +403,84 @@ struct Producer {
     for (int i = ptid; i < G::HG_R * G::HG_C; i += G::NP) {
       const int kyl = i / G::HG_C, kxl = i % G::HG_C;
       const int ky = u.kb_y + kyl, kx = u.kb_x + kxl;
-      float nxv[FP], nyv[FP];
+      const bool valid = ky >= 1 && ky <= u.kmax_y && kx >= 1 && kx <= u.kmax_x;
+      float gx[FP], gy[FP];
 #pragma unroll
-      for (int fr = 0; fr < FP; ++fr) nxv[fr] = nyv[fr] = 0.f;
-      if (ky >= 1 && ky <= u.kmax_y && kx >= 1 && kx <= u.kmax_x) {
-        float gx[FP], gy[FP];
-        if (ky >= twoH) {
+      for (int fr = 0; fr < FP; ++fr) gx[fr] = gy[fr] = 0.f;
+      if (valid) {
+        if constexpr (FP >= 2) {
 #pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* c0 = t1 + (2 * fr) * G::S_T1 + kxl;
-            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + kxl;
-            gx[fr] = gy[fr] = 0.f;
+          for (int pp = 0; pp < FP / 2; ++pp) {
+            const float4* c4 = reinterpret_cast<const float4*>(t1) + pp * G::S_T1 + kxl;
+            float2 x = make_float2(0.f, 0.f), y = make_float2(0.f, 0.f);
+            if (ky >= twoH) {
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const float4 q = c4[(p.cy_base + t - u.RY0) * G::HG_C];
+                const float2 w = make_float2(p.cy[t], p.cy[t]);
+                x = __ffma2_rn(w, make_float2(q.x, q.y), x);
+                y = __ffma2_rn(w, make_float2(q.z, q.w), y);
+              }
+            } else if (ky & 1) {
+              const float4 q = c4[(((ky - 1) >> 1) - u.RY0) * G::HG_C];
+              x = make_float2(q.x, q.y);
+              y = make_float2(q.z, q.w);
+            } else {
+              const float4* c = c4 + ((ky >> 1) - 2 - u.RY0) * G::HG_C;
+              const float2 c0 = make_float2(-0.0625f, -0.0625f);
+              const float2 c1 = make_float2(0.5625f, 0.5625f);
+              const float4 q0 = c[0], q1 = c[G::HG_C], q2 = c[2 * G::HG_C], q3 = c[3 * G::HG_C];
+              x = __fmul2_rn(c0, make_float2(q0.x, q0.y));
+              y = __fmul2_rn(c0, make_float2(q0.z, q0.w));
+              x = __ffma2_rn(c1, make_float2(q1.x, q1.y), x);
+              y = __ffma2_rn(c1, make_float2(q1.z, q1.w), y);
+              x = __ffma2_rn(c1, make_float2(q2.x, q2.y), x);
+              y = __ffma2_rn(c1, make_float2(q2.z, q2.w), y);
+              x = __ffma2_rn(c0, make_float2(q3.x, q3.y), x);
+              y = __ffma2_rn(c0, make_float2(q3.z, q3.w), y);
+            }
+            gx[2 * pp] = x.x;
+            gx[2 * pp + 1] = x.y;
+            gy[2 * pp] = y.x;
+            gy[2 * pp + 1] = y.y;
+          }
+        } else {
+          const float* c0 = t1 + kxl;
+          const float* c1 = t1 + G::S_T1 + kxl;
+          if (ky >= twoH) {
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
               const int rl = p.cy_base + t - u.RY0;
-              gx[fr] = fmaf(p.cy[t], c0[rl * G::HG_C], gx[fr]);
-              gy[fr] = fmaf(p.cy[t], c1[rl * G::HG_C], gy[fr]);
+              gx[0] = fmaf(p.cy[t], c0[rl * G::HG_C], gx[0]);
+              gy[0] = fmaf(p.cy[t], c1[rl * G::HG_C], gy[0]);
             }
-          }
-        } else if (ky & 1) {
-          const int rl = ((ky - 1) >> 1) - u.RY0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            gx[fr] = t1[(2 * fr) * G::S_T1 + rl * G::HG_C + kxl];
-            gy[fr] = t1[(2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl];
-          }
-        } else {
-          const int rl = (ky >> 1) - 2 - u.RY0;
-#pragma unroll
-          for (int fr = 0; fr < FP; ++fr) {
-            const float* c0 = t1 + (2 * fr) * G::S_T1 + rl * G::HG_C + kxl;
-            const float* c1 = t1 + (2 * fr + 1) * G::S_T1 + rl * G::HG_C + kxl;
-            float x = -0.0625f * c0[0], y = -0.0625f * c1[0];
-            x = fmaf(0.5625f, c0[G::HG_C], x);
-            y = fmaf(0.5625f, c1[G::HG_C], y);
-            x = fmaf(0.5625f, c0[2 * G::HG_C], x);
-            y = fmaf(0.5625f, c1[2 * G::HG_C], y);
-            gx[fr] = fmaf(-0.0625f, c0[3 * G::HG_C], x);
-            gy[fr] = fmaf(-0.0625f, c1[3 * G::HG_C], y);
+          } else if (ky & 1) {
+            const int rl = ((ky - 1) >> 1) - u.RY0;
+            gx[0] = c0[rl * G::HG_C];
+            gy[0] = c1[rl * G::HG_C];
+          } else {
+            const int rl = (ky >> 1) - 2 - u.RY0;
+            const float* a0 = c0 + rl * G::HG_C;
+            const float* a1 = c1 + rl * G::HG_C;
+            float x = -0.0625f * a0[0], y = -0.0625f * a1[0];
+            x = fmaf(0.5625f, a0[G::HG_C], x);
+            y = fmaf(0.5625f, a1[G::HG_C], y);
+            x = fmaf(0.5625f, a0[2 * G::HG_C], x);
+            y = fmaf(0.5625f, a1[2 * G::HG_C], y);
+            gx[0] = fmaf(-0.0625f, a0[3 * G::HG_C], x);
+            gy[0] = fmaf(-0.0625f, a1[3 * G::HG_C], y);
           }
         }
+      }
+      float nxv[FP], nyv[FP];
 #pragma unroll
-        for (int fr = 0; fr < FP; ++fr) {
-          const float m2 = fmaf(gx[fr], gx[fr], gy[fr] * gy[fr]);
-          if (m2 > 0.f) {
-            const float inv = rsqrtf(m2);
-            nxv[fr] = gx[fr] * inv;
-            nyv[fr] = gy[fr] * inv;
-          }
+      for (int fr = 0; fr < FP; ++fr) {
+        nxv[fr] = nyv[fr] = 0.f;
+        const float m2 = fmaf(gx[fr], gx[fr], gy[fr] * gy[fr]);
+        if (valid && m2 > 0.f) {
+          const float inv = rsqrtf(m2);
+          nxv[fr] = gx[fr] * inv;
+          nyv[fr] = gy[fr] * inv;
         }
       }
       const int o = (kyl * 2 + (kxl & 1)) * G::HGP + (kxl >> 1);
