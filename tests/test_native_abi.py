@@ -124,3 +124,12 @@ def test_argument_checks_run_before_any_device_work(lib):
     assert lib.nx_fht_plan_create(ctypes.byref(h), 8, 8, 0) == _native.NX_ERR_INVALID_ARG
     assert lib.nx_fht_interpolate(None, None, 1, None, None, 0, None) == \
         _native.NX_ERR_INVALID_ARG
+    # eSRRF-3D: the slice index of a window sample is formed by a multiply-high
+    # that is exact while S * magnification_z^2 < 2^32; deeper stacks are
+    # refused on the host (the pointers here are never dereferenced)
+    big = ctypes.c_size_t(2 ** 63)
+    assert lib.nx_esrrf3d_st(P(256), 1, 65536, 8, 8, 1, 256, 1.5, 1.05, 1.0, 0, 1, P(256),
+                             P(256), big, None) == _native.NX_ERR_INVALID_ARG
+    assert b"2^32" in lib.nx_last_error()
+    assert lib.nx_esrrf3d_st(P(256), 1, 4, 8, 8, 0, 2, 1.5, 1.05, 1.0, 0, 1, P(256), P(256),
+                             big, None) == _native.NX_ERR_INVALID_ARG
