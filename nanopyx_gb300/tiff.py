@@ -5,9 +5,9 @@ The reference's CLI reads and writes TIFF through ``tifffile``
 installed.  Otherwise this module's own baseline-TIFF codec serves:
 
 * read: classic and BigTIFF, either byte order, every page (IFD) of the file,
-  strips or tiles, no compression / Deflate (zlib) / PackBits, optionally
-  with horizontal differencing, 8/16/32/64-bit unsigned, signed and float
-  samples, one sample per pixel; pages of one shape stack to (pages, H, W),
+  strips or tiles, no compression / LZW / Deflate (zlib) / PackBits, with
+  horizontal differencing (predictor 2) or the floating-point predictor (3),
+  8/16/32/64-bit unsigned, signed and float samples, one sample per pixel; pages of one shape stack to (pages, H, W),
   and an ImageJ description or a ``{"shape": [...]}`` JSON description
   restores the array's shape.
 * write: little-endian uncompressed TIFF (BigTIFF past 4 GB), one page per
@@ -149,6 +149,47 @@ def _unpackbits(buf: bytes, expected: int) -> bytes:
     return bytes(out)
 
 
+def _lzw_decode(buf: bytes, expected: int) -> bytes:
+    """TIFF LZW (TIFF 6.0 section 13): MSB-first codes of 9 to 12 bits,
+    256 = clear, 257 = end of information, the code width growing one code
+    early (after table entries 510, 1022 and 2046)."""
+    src = bytes(buf) + b"\0\0\0\0"
+    nbits = len(buf) * 8
+    out = bytearray()
+    table = [bytes((i,)) for i in range(256)] + [b"", b""]
+    width, pos, prev = 9, 0, None
+    while pos + width <= nbits and len(out) < expected:
+        i = pos >> 3
+        word = (src[i] << 24) | (src[i + 1] << 16) | (src[i + 2] << 8) | src[i + 3]
+        code = (word >> (32 - (pos & 7) - width)) & ((1 << width) - 1)
+        pos += width
+        if code == 257:
+            break
+        if code == 256:
+            del table[258:]
+            width, prev = 9, None
+            continue
+        if prev is None:
+            if code >= 256:
+                raise ValueError("corrupt TIFF LZW data")
+            entry = table[code]
+        else:
+            if code < len(table):
+                entry = table[code]
+                new_entry = prev + entry[:1]
+            elif code == len(table):
+                entry = new_entry = prev + prev[:1]
+            else:
+                raise ValueError("corrupt TIFF LZW data")
+            if len(table) < 4096:
+                table.append(new_entry)
+                if len(table) + 1 >= (1 << width) and width < 12:
+                    width += 1
+        out += entry
+        prev = entry
+    return bytes(out)
+
+
 def _read_page(data, tags, bo) -> np.ndarray:
     W = tags[256][0]
     H = tags[257][0]
@@ -157,14 +198,16 @@ def _read_page(data, tags, bo) -> np.ndarray:
     spp = tags.get(277, (1,))[0]
     fmt = _SAMPLE.get(tags.get(339, (1,))[0])
     pred = tags.get(317, (1,))[0]
-    if pred not in (1, 2):
+    if pred not in (1, 2, 3):
         raise NotImplementedError(f"TIFF predictor {pred} (install tifffile)")
     if spp != 1:
         raise NotImplementedError("TIFF pages with more than one sample per pixel")
     if fmt is None or bits not in (8, 16, 32, 64):
         raise NotImplementedError(f"TIFF samples of {bits} bits, format {tags.get(339)}")
-    if comp not in (1, 8, 32946, 32773):
+    if comp not in (1, 5, 8, 32946, 32773):
         raise NotImplementedError(f"TIFF compression {comp} (install tifffile)")
+    if pred == 3 and fmt != "f":
+        raise ValueError("TIFF floating-point predictor on non-float samples")
     dt = np.dtype(f"{bo}{fmt}{bits // 8}")
 
     def chunk(offset, count, nbytes):
@@ -173,7 +216,22 @@ def _read_page(data, tags, bo) -> np.ndarray:
             raw = zlib.decompress(raw)
         elif comp == 32773:
             raw = _unpackbits(raw, nbytes)
+        elif comp == 5:
+            raw = _lzw_decode(raw, nbytes)
         return raw[:nbytes]
+
+    def block(raw, rows, width):
+        # one strip or tile as a (rows, width) array, the predictor undone
+        if pred == 3:
+            # floating-point predictor (Adobe TIFF technical note 3): each row
+            # holds the samples' bytes most significant first, byte plane by
+            # byte plane, horizontally differenced as bytes
+            b = np.frombuffer(raw, dtype=np.uint8).reshape(rows, dt.itemsize * width)
+            b = np.cumsum(b, axis=1, dtype=np.uint8).reshape(rows, dt.itemsize, width)
+            b = np.ascontiguousarray(b.transpose(0, 2, 1))
+            return b.view(dt.newbyteorder(">")).reshape(rows, width).astype(dt)
+        a = np.frombuffer(raw, dtype=dt).reshape(rows, width)
+        return np.cumsum(a, axis=1, dtype=dt) if pred == 2 else a
 
     if 322 in tags:  # tiled
         tw, tl = tags[322][0], tags[323][0]
@@ -181,9 +239,7 @@ def _read_page(data, tags, bo) -> np.ndarray:
         img = np.zeros((H, W), dtype=dt)
         across = -(-W // tw)
         for k, (o, c) in enumerate(zip(offs, cnts)):
-            t = np.frombuffer(chunk(o, c, tw * tl * dt.itemsize), dtype=dt).reshape(tl, tw)
-            if pred == 2:
-                t = np.cumsum(t, axis=1, dtype=dt)
+            t = block(chunk(o, c, tw * tl * dt.itemsize), tl, tw)
             r0, c0 = (k // across) * tl, (k % across) * tw
             h, w = min(tl, H - r0), min(tw, W - c0)
             img[r0:r0 + h, c0:c0 + w] = t[:h, :w]
@@ -195,11 +251,8 @@ def _read_page(data, tags, bo) -> np.ndarray:
         parts = []
         for k, (o, c) in enumerate(zip(offs, cnts)):
             rows = min(rps, H - k * rps)
-            parts.append(np.frombuffer(chunk(o, c, rows * W * dt.itemsize),
-                                       dtype=dt).reshape(rows, W))
+            parts.append(block(chunk(o, c, rows * W * dt.itemsize), rows, W))
         img = np.concatenate(parts, axis=0)
-        if pred == 2:
-            img = np.cumsum(img, axis=1, dtype=dt)
     return img.astype(dt.newbyteorder("="))
 
 
