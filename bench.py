@@ -40,7 +40,7 @@ CFG = dict(T=500, H=512, W=512, emitters=400, m=5, radius=1.5, sensitivity=2.0,
 SMALL = dict(T=160, fpt=80)
 # DRAM bytes of one fused launch, dram__bytes_read.sum + dram__bytes_write.sum from a
 # 1-pass ncu capture of that launch (large: the full 500-frame launch; small: 160 frames)
-TRAFFIC_BYTES = {"large": 531461120 + 604324352, "small": 169977088 + 207399936}
+TRAFFIC_BYTES = {"large": 531373568 + 603790336, "small": 168473856 + 207223296}
 METRIC = "eSRRF input Mpx*frames/s"
 # frames per reference step: eSRRF_ST and the temporal step scale with the frame
 # count; the per-timepoint macro-pixel correction (2 x ~30 ms on 2560^2) is <1 %
