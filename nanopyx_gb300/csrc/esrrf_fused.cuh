@@ -10,7 +10,8 @@
 //   3. Catmull-Rom-interpolate the gradients on the half-pixel grid -- the only
 //      positions the reference RGC ever reads from its 2m-magnified gradient
 //      images (rows/cols k*m, clamped to 2*m*H-1;
-//      _c_sr_radial_gradient_convergence.c:45-61) -- and normalise them into a
+//      _c_sr_radial_gradient_convergence.c:45-61) -- on packed f32x2
+//      arithmetic over the frame pair, and normalise them into a
 //      double-buffered slot;
 // while its consumer warps, one thread per input pixel and output row phase,
 //   4. evaluate RGC for the thread's M output pixels with FP64-derived phase
