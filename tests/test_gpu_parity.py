@@ -5,6 +5,8 @@ tolerance the eSRRF/SRRF path is held to; integer-exact steps (Roberts-Cross)
 are compared bit for bit.  Every call goes through the package, which calls the
 C ABI of libnanopyx_gb300.so.
 """
+import warnings
+
 import numpy as np
 import pytest
 import torch
@@ -207,6 +209,23 @@ def test_timepoints_equal_separate_calls():
     for i, (a, b) in enumerate(((0, 12), (12, 24), (24, 30))):
         one = nx.eSRRF(x[a:b], 4, 2.0, 2, temporal_correlation="TAC2")
         assert rel_err(full[i], one) <= 1e-5
+
+
+def test_one_frame_tail_timepoint_like_the_reference():
+    """A last timepoint of one frame: the reference's VAR is 0 there and its TAC2
+    the mean of an empty lag product, NaN at every pixel (NaN through the
+    macro-pixel correction too); the full timepoint matches the oracle."""
+    x = blinking_stack(11, 20, 24, 6, seed=9)
+    var, tac2 = nx.eSRRF(x, 2, 1.5, 1, frames_per_timepoint=10,
+                         temporal_correlation=("VAR", "TAC2"))
+    assert var.shape == tac2.shape == (2, 40, 48)
+    assert np.all(var[1] == 0) and np.all(np.isnan(tac2[1]))
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)  # the oracle's empty-slice mean
+        for got, name in ((var, "VAR"), (tac2, "TAC2")):
+            ref = O.esrrf(x, 2, 1.5, 1, 10, name)
+            assert np.isnan(ref[1]).all() == (name == "TAC2")
+            assert rel_err(got[0], ref[0]) <= TOL, name
 
 
 def test_cfg0_against_reference():
