@@ -172,3 +172,21 @@ def test_brent_search_agrees_with_scipy():
             assert abs(g - ref) <= 1e-6 * max(1.0, abs(ref))
         else:
             assert g <= 0.0 and ref <= 0.0
+
+
+@pytest.mark.parametrize("shape,kw", [((2, 2, 8, 8), dict(radius=1.5, PSF_ratio=2.8, voxel_ratio=4.0)),
+                                      ((2, 6, 8, 8), dict(radius=2.5)),
+                                      ((8, 8), {}), ((2, 3, 4, 8, 8), {})])
+def test_esrrf3d_declines_like_the_reference(shape, kw, capsys):
+    """_le_esrrf3d.pyx:42-61: a wrong rank or a radius too large for the
+    volume prints the reference's warning and returns None (host side, before
+    any device work); the reference itself is compared where it is built."""
+    x = np.zeros(shape, np.float32)
+    assert nx.eSRRF3D_ST(verbose=False).run(x, **kw) is None
+    ours = capsys.readouterr().out
+    assert ours.startswith("Warning")
+    from oracle import ref_build
+
+    if ref_build.available():
+        ref = ref_build.load()["eSRRF3D_ST"](verbose=False).run(x, run_type="Threaded", **kw)
+        assert ref is None and capsys.readouterr().out == ours
