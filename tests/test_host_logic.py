@@ -178,7 +178,7 @@ def test_brent_search_agrees_with_scipy():
                                       ((2, 6, 8, 8), dict(radius=2.5)),
                                       ((8, 8), {}), ((2, 3, 4, 8, 8), {})])
 def test_esrrf3d_declines_like_the_reference(shape, kw, capsys):
-    """_le_esrrf3d.pyx:42-61: a wrong rank or a radius too large for the
+    """_le_esrrf3d.pyx:36-48: a wrong rank or a radius too large for the
     volume prints the reference's warning and returns None (host side, before
     any device work); the reference itself is compared where it is built."""
     x = np.zeros(shape, np.float32)
